@@ -1,0 +1,224 @@
+/*
+ * steps_gb300.h -- C-ABI of libsteps_gb300.so, a GB300-native (sm_103a)
+ * implementation of the StePS direct O(N^2) gravity force evaluation.
+ *
+ * The library replaces the three direct-summation force functions of StePS
+ * behind their own interface:
+ *
+ *   void forces(REAL* x, REAL* F, int ID_min, int ID_max);             R^3
+ *        StePS/src/forces.cc:510, StePS/src/forces_cuda.cu:74
+ *   void forces_periodic(REAL* x, REAL* F, int ID_min, int ID_max);    T^3
+ *        StePS/src/forces.cc:776, StePS/src/forces_cuda.cu:169
+ *   void forces_periodic_z(REAL* x, REAL* F, int ID_min, int ID_max);  S1xR2
+ *        StePS/src/forces.cc:1221, StePS/src/forces_cuda.cu:457
+ *
+ * Those three symbols themselves are provided, on top of this C-ABI, by
+ * steps_gb300/legacy/forces_gb300.cc, which reads the StePS globals
+ * (N, M, SOFT_LENGTH, L, Rsim, IS_PERIODIC, COSMOLOGY, ... declared in
+ * StePS/src/global_variables.h:42-147) and is linked into the unchanged
+ * StePS driver in place of forces.cc / forces_cuda.cu.
+ *
+ * Conventions (all entry points):
+ *   - every call returns an int status (STEPS_OK = 0); the text of the last
+ *     failure is available from steps_gpu_error_string();
+ *   - positions x are AoS double[3*n] (x[3*i+k]), the layout of the StePS
+ *     global x (StePS/src/global_variables.h:107);
+ *   - forces are accelerations with G = 1, OVERWRITTEN (not accumulated) for
+ *     i in [id_min, id_max] and stored at F[3*(i-id_min)+k], as
+ *     forces.cc:520-526 and forces_cuda.cu:1045,1078-1097 return them;
+ *   - one GPU, one internal CUDA stream; calls are synchronous from the
+ *     caller's view (unless documented otherwise) and not re-entrant.
+ */
+#ifndef STEPS_GB300_H
+#define STEPS_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define STEPS_GB300_ABI_VERSION 1
+
+/* Status codes. */
+#define STEPS_OK 0
+#define STEPS_E_ARG 1     /* invalid argument: null pointer, bad size or range */
+#define STEPS_E_STATE 2   /* call out of order: not initialised, no particles, no table */
+#define STEPS_E_CUDA 3    /* a CUDA runtime call or kernel launch failed */
+#define STEPS_E_NOMEM 4   /* device allocation failed */
+#define STEPS_E_TABLE 5   /* table shape does not match the request */
+#define STEPS_E_TIMEOUT 6 /* a bounded device-side wait gave up (status written by the kernel) */
+
+/* Topologies (compile-time PERIODIC / PERIODIC_Z switches in StePS,
+ * StePS/Template-LinuxGCC-Makefile:29-32). */
+#define STEPS_R3 0   /* compactified non-periodic R^3 */
+#define STEPS_T3 1   /* T^3: nearest image + Ewald correction table */
+#define STEPS_S1R2 2 /* S1xR2: periodic along z */
+
+/* Precision modes. */
+#define STEPS_FP64 0  /* plain FP64 end to end (correctness reference on the GPU) */
+#define STEPS_MIXED 1 /* FP32 pair arithmetic on tile-centred coordinates, FP64 accumulation */
+
+/* Per-call physics parameters: the StePS globals the force functions read.
+ * Mirrors StePS/src/global_variables.h:42-47,98,104,118-147. */
+typedef struct steps_params {
+    int topology;               /* STEPS_R3 / STEPS_T3 / STEPS_S1R2 */
+    int is_periodic;            /* IS_PERIODIC: T3 1 = nearest image only, >= 2 Ewald table;
+                                   S1R2: 1 = nearest image, >= 2 periodic images / table */
+    double L;                   /* L: box size (T3) or periodic length L_z (S1R2) */
+    double rsim;                /* Rsim: radius of the simulation volume */
+    int cosmology;              /* COSMOLOGY */
+    int comoving;               /* COMOVING_INTEGRATION */
+    double mass_in_unit_sphere; /* mass_in_unit_sphere (background pull, comoving runs) */
+    double h0;                  /* H0 (non-comoving background term H0^2 * Omega_lambda) */
+    double omega_lambda;        /* Omega_lambda */
+    int ewald_order;            /* T3: 2 (trilinear) or 4 (Catmull-Rom tricubic);
+                                   S1R2 table: 0 (NGP), 2 (CIC), 4 (TSC) -- EWALD_INTERPOLATION_ORDER */
+    int s1r2_images;            /* S1R2 with is_periodic >= 2: 1 = explicit image sum
+                                   (PERIODIC_Z_NOLOOKUP), 0 = (rho, z) correction table */
+} steps_params;
+
+/* ---- lifetime ----------------------------------------------------------- */
+
+/* Selects the GPU and creates the persistent device context (stream, events,
+ * buffers). Replaces the per-call cudaSetDevice/cudaMalloc/cudaFree of
+ * forces_cuda.cu:959-1105. Idempotent for the same device. */
+int steps_gpu_init(int device);
+
+/* Frees every device buffer and the stream. Safe to call twice. */
+int steps_gpu_shutdown(void);
+
+/* Text of the last failure on this thread ("" if none). Never NULL. */
+const char *steps_gpu_error_string(void);
+
+int steps_gpu_abi_version(void);
+
+/* ---- particle data ------------------------------------------------------ */
+
+/* Uploads the per-particle masses M[n] and softening lengths SOFT_LENGTH[n]
+ * (host arrays, StePS/src/global_variables.h:98-99; softening from
+ * calculate_softening_length, StePS/src/utils.cc:59-82). Call again whenever
+ * either changes; n fixes the particle count for the following force calls. */
+int steps_gpu_set_particles(int n, const double *m, const double *eps);
+
+/* ---- tables ------------------------------------------------------------- */
+
+/* T^3 Ewald correction table D(r) on the cell-centred ngrid^3 grid over
+ * [-L/2, L/2]^3, layout table[((ix*ngrid+iy)*ngrid+iz)*3+c]
+ * (T3_EWALD_FORCE_TABLE, StePS/src/ewald_space.cc:45-48, :288). Host FP64. */
+int steps_gpu_set_table_t3(int ngrid, const double *table);
+
+/* Builds the T^3 table on the GPU in FP64 (StePS/src/ewald_space.cc:210-383
+ * computed at every grid point): real-space images n with |n|^2 < real_radius^2
+ * and |r + nL| <= rel_cut*L; reciprocal vectors h with |h|^2 < rec_radius^2 and
+ * |2 pi h / L| <= rec_cut; Ewald parameter alpha. main.cc:416-470 uses
+ * alpha = 2/L, real_radius = rel_cut + 1, rec_radius = rec_cut + 2. */
+int steps_gpu_build_table_t3(int ngrid, double L, double alpha, double rel_cut, double rec_cut, double real_radius,
+                             double rec_radius);
+
+/* Copies the current T^3 table (ngrid^3*3 doubles) to the host. */
+int steps_gpu_get_table_t3(double *out);
+
+/* S1xR2 (rho, z) correction table, layout table[(ir*nz+iz)*2+c], c = 0: D_rho,
+ * 1: D_z (S1R2_EWALD_FORCE_TABLE, StePS/src/ewald_space.cc:612-616, :754). */
+int steps_gpu_set_table_s1r2(int nrho, int nz, const double *table);
+
+/* Builds the S1xR2 table on the GPU (StePS/src/ewald_space.cc:618-798,
+ * Tornberg 2015 singly periodic Ewald sums) for rho in [0, rho_max]. */
+int steps_gpu_build_table_s1r2(int nrho, int nz, double rho_max, double lz, double alpha, int nmax, int mmax);
+int steps_gpu_get_table_s1r2(double *out);
+
+/* Cylindrical background multiplier table RADIAL_FORCE_TABLE[size]
+ * (StePS/src/utils.cc:162-228), used by S1xR2 comoving runs. */
+int steps_gpu_set_radial_table(int size, const double *table);
+
+/* ---- force evaluation --------------------------------------------------- */
+
+/* The drop-in force call with HOST buffers: uploads x (double[3n]), computes
+ * the accelerations of particles id_min..id_max against all n particles and
+ * downloads them into F (double[3*(id_max-id_min+1)], overwritten).
+ * Equivalent of forces()/forces_periodic()/forces_periodic_z()
+ * (forces.cc:510/776/1221, forces_cuda.cu:878/1121/1378). */
+int steps_gpu_forces(const steps_params *p, int precision, const double *x, double *F, int id_min, int id_max);
+
+/* Device-resident variant: positions already uploaded with
+ * steps_gpu_upload_positions (or advanced by steps_gpu_kdk); the result
+ * stays on the device until steps_gpu_download_forces. No host copies. */
+int steps_gpu_upload_positions(const double *x);
+int steps_gpu_forces_resident(const steps_params *p, int precision, int id_min, int id_max);
+int steps_gpu_download_forces(double *F);
+
+/* ---- leapfrog (device resident) ----------------------------------------- */
+
+/* Uploads velocities v[3n] (host). */
+int steps_gpu_upload_velocities(const double *v);
+
+/* nsteps fixed-h KDK steps of StePS's step() (StePS/src/step.cc:100-312) on
+ * the resident x, v: kick h/2 + drift h, periodic wrap, force, kick h/2, with
+ * acceleration g*F*a^-3 - 2*hubble*v. Computes the forces of the current
+ * positions first if none are resident. errmax (step.cc:265-269, with
+ * rho_part) of the last step is written to *errmax_out when non-NULL. */
+int steps_gpu_kdk(const steps_params *p, int precision, int nsteps, double h, double g, double a, double hubble,
+                  double rho_part, double *errmax_out);
+
+/* Downloads the resident positions, velocities and forces (any may be NULL). */
+int steps_gpu_download_state(double *x, double *v, double *F);
+
+/* ---- batched ensembles (independent realisations, uneven N) ------------- */
+
+/* Registers `count` independent R^3 realisations; realisation k has n[k]
+ * particles whose positions, masses and softening lengths are the host arrays
+ * x[k] (double[3 n[k]]), m[k], eps[k]. */
+int steps_gpu_batch_set(int count, const int *n, const double *const *x, const double *const *m,
+                        const double *const *eps);
+
+/* One force evaluation followed by nsteps fixed-h KDK steps of every
+ * realisation. graph = 1 runs it as one persistent work-queue kernel per
+ * phase captured into a CUDA graph (autotuned tile shape and block count);
+ * graph = 0 runs it as `count` separate plain launches per phase. */
+int steps_gpu_batch_run(const steps_params *p, int precision, int nsteps, double h, int graph);
+
+/* Downloads realisation k's positions/velocities/forces (any may be NULL). */
+int steps_gpu_batch_get(int k, double *x, double *v, double *F);
+
+/* ---- tuning and instrumentation ----------------------------------------- */
+
+/* Fixes the mixed-precision kernel shape: threads per block (64/128/256),
+ * i-particles per thread (1/2/4) and j-range split (0 = automatic). Tile size
+ * is threads*ipt. Returns STEPS_E_ARG for an unsupported shape. */
+int steps_gpu_set_tuning(int threads, int ipt, int jsplit);
+
+/* Times every supported mixed-precision shape on the resident particles for
+ * the given topology and keeps the fastest; writes threads, ipt to out[2]. */
+int steps_gpu_autotune(const steps_params *p, int id_min, int id_max, int *out);
+
+/* Number of kernels this library has launched since init. */
+long long steps_gpu_launch_count(void);
+
+/* Device time (CUDA events on the library stream) of the phases of the last
+ * force evaluation: 0 = preparation (packing, ordering, tiling), 1 = pair
+ * kernel, 2 = reduction/epilogue. Synchronises the stream. */
+double steps_gpu_last_phase_ms(int phase);
+
+/* Pairs the last pair kernel evaluated: (id_max-id_min+1) * n. */
+double steps_gpu_last_pairs(void);
+
+/* Event markers on the library stream for callers that time a sequence of
+ * calls: mark(slot) records event `slot` (0..15); elapsed(a, b) synchronises
+ * and returns milliseconds between two recorded marks. */
+int steps_gpu_timer_mark(int slot);
+double steps_gpu_timer_elapsed_ms(int a, int b);
+
+/* Overwrites a device buffer of `bytes` bytes on the library stream (evicts
+ * L2 between timed steps). */
+int steps_gpu_flush_l2(long long bytes);
+
+/* Measures this GPU's FP32 FMA and FP64 FMA issue peaks (FLOP/s, an FMA
+ * counted as 2) with dependent-chain kernels; either pointer may be NULL. */
+int steps_gpu_measure_peaks(double *fp32_flops, double *fp64_flops);
+
+/* Blocks until the library stream is idle; returns a pending kernel error. */
+int steps_gpu_synchronize(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* STEPS_GB300_H */

@@ -1,0 +1,212 @@
+"""steps_gb300: GB300-native (sm_103a) StePS direct-summation force evaluation.
+
+The product is the C-ABI shared library ``libsteps_gb300.so`` (declared in
+include/steps_gb300.h). This package is a thin ctypes front end used by the
+tests and the benchmark; it loads the in-tree library and fails loudly when
+it is missing -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import workloads  # noqa: F401
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "_build", "libsteps_gb300.so")
+
+STEPS_OK, STEPS_E_ARG, STEPS_E_STATE, STEPS_E_CUDA, STEPS_E_NOMEM, STEPS_E_TABLE, STEPS_E_TIMEOUT = range(7)
+R3, T3, S1R2 = 0, 1, 2
+FP64, MIXED = 0, 1
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+class StepsError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"steps_gb300 error {code}: {msg}")
+        self.code = code
+
+
+class Params(C.Structure):
+    """Mirror of ``steps_params`` (include/steps_gb300.h)."""
+
+    _fields_ = [("topology", C.c_int), ("is_periodic", C.c_int), ("L", C.c_double), ("rsim", C.c_double),
+                ("cosmology", C.c_int), ("comoving", C.c_int), ("mass_in_unit_sphere", C.c_double),
+                ("h0", C.c_double), ("omega_lambda", C.c_double), ("ewald_order", C.c_int),
+                ("s1r2_images", C.c_int)]
+
+
+def params(topology=R3, is_periodic=0, L=0.0, rsim=0.0, cosmology=0, comoving=0, mius=0.0, h0=0.0, oml=0.0,
+           ewald_order=4, s1r2_images=1) -> Params:
+    return Params(topology, is_periodic, L, rsim, cosmology, comoving, mius, h0, oml, ewald_order, s1r2_images)
+
+
+_LIB = None
+
+
+def load_library(path: str = LIB_PATH) -> C.CDLL:
+    """Loads libsteps_gb300.so; raises if it has not been built."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = C.CDLL(path)
+    lib.steps_gpu_error_string.restype = C.c_char_p
+    lib.steps_gpu_launch_count.restype = C.c_longlong
+    lib.steps_gpu_last_phase_ms.restype = C.c_double
+    lib.steps_gpu_last_pairs.restype = C.c_double
+    lib.steps_gpu_timer_elapsed_ms.restype = C.c_double
+    lib.steps_gpu_flush_l2.argtypes = [C.c_longlong]
+    for name in ("steps_gpu_build_table_t3",):
+        getattr(lib, name).argtypes = [C.c_int] + [C.c_double] * 6
+    lib.steps_gpu_build_table_s1r2.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int,
+                                               C.c_int]
+    lib.steps_gpu_kdk.argtypes = [C.POINTER(Params), C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                                  C.c_double, C.c_double, _dp]
+    lib.steps_gpu_forces.argtypes = [C.POINTER(Params), C.c_int, _dp, _dp, C.c_int, C.c_int]
+    lib.steps_gpu_forces_resident.argtypes = [C.POINTER(Params), C.c_int, C.c_int, C.c_int]
+    lib.steps_gpu_batch_run.argtypes = [C.POINTER(Params), C.c_int, C.c_int, C.c_double, C.c_int]
+    _LIB = lib
+    return lib
+
+
+def _d(a: np.ndarray):
+    return a.ctypes.data_as(_dp)
+
+
+class Engine:
+    """Host-side handle on the library's single-GPU context.
+
+    Mirrors the reference force interface: positions x (N,3) float64 in,
+    accelerations of particles id_min..id_max out (overwritten)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load_library()
+        self._check(self.lib.steps_gpu_init(int(device)))
+        self.n = 0
+
+    def _check(self, rc: int):
+        if rc != STEPS_OK:
+            raise StepsError(rc, self.lib.steps_gpu_error_string().decode())
+
+    def shutdown(self):
+        self._check(self.lib.steps_gpu_shutdown())
+
+    def set_particles(self, m, eps):
+        m = np.ascontiguousarray(m, dtype=np.float64)
+        eps = np.ascontiguousarray(eps, dtype=np.float64)
+        self._check(self.lib.steps_gpu_set_particles(int(m.size), _d(m), _d(eps)))
+        self.n = int(m.size)
+
+    def forces(self, x, p: Params, precision=MIXED, id_min=0, id_max=None) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        if id_max is None:
+            id_max = self.n - 1
+        F = np.empty((id_max - id_min + 1, 3))
+        self._check(self.lib.steps_gpu_forces(C.byref(p), int(precision), _d(x), _d(F), int(id_min), int(id_max)))
+        return F
+
+    def upload_positions(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        self._check(self.lib.steps_gpu_upload_positions(_d(x)))
+
+    def upload_velocities(self, v):
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        self._check(self.lib.steps_gpu_upload_velocities(_d(v)))
+
+    def forces_resident(self, p: Params, precision=MIXED, id_min=0, id_max=None):
+        if id_max is None:
+            id_max = self.n - 1
+        self._check(self.lib.steps_gpu_forces_resident(C.byref(p), int(precision), int(id_min), int(id_max)))
+        self._last_ni = id_max - id_min + 1
+
+    def download_forces(self, ni=None) -> np.ndarray:
+        ni = ni or self._last_ni
+        F = np.empty((ni, 3))
+        self._check(self.lib.steps_gpu_download_forces(_d(F)))
+        return F
+
+    def kdk(self, p: Params, precision, nsteps, h, g=1.0, a=1.0, hubble=0.0, rho_part=1.0) -> float:
+        e = C.c_double(0)
+        self._check(self.lib.steps_gpu_kdk(C.byref(p), int(precision), int(nsteps), float(h), float(g), float(a),
+                                           float(hubble), float(rho_part), C.byref(e)))
+        return e.value
+
+    def state(self):
+        x = np.empty((self.n, 3)); v = np.empty((self.n, 3)); F = np.empty((self.n, 3))
+        self._check(self.lib.steps_gpu_download_state(_d(x), _d(v), _d(F)))
+        return x, v, F
+
+    # tables
+    def set_table_t3(self, table, ngrid):
+        table = np.ascontiguousarray(table, dtype=np.float64)
+        self._check(self.lib.steps_gpu_set_table_t3(int(ngrid), _d(table)))
+
+    def build_table_t3(self, ngrid, L, alpha, rel_cut, rec_cut, real_radius, rec_radius):
+        self._check(self.lib.steps_gpu_build_table_t3(int(ngrid), L, alpha, rel_cut, rec_cut, real_radius,
+                                                      rec_radius))
+        self.t3_ng = int(ngrid)
+
+    def get_table_t3(self, ngrid=None):
+        ngrid = ngrid or self.t3_ng
+        out = np.empty(3 * ngrid ** 3)
+        self._check(self.lib.steps_gpu_get_table_t3(_d(out)))
+        return out
+
+    def set_table_s1r2(self, table, nrho, nz):
+        table = np.ascontiguousarray(table, dtype=np.float64)
+        self._check(self.lib.steps_gpu_set_table_s1r2(int(nrho), int(nz), _d(table)))
+
+    def build_table_s1r2(self, nrho, nz, rho_max, lz, alpha, nmax, mmax):
+        self._check(self.lib.steps_gpu_build_table_s1r2(int(nrho), int(nz), rho_max, lz, alpha, int(nmax),
+                                                        int(mmax)))
+        self.s1r2_shape = (int(nrho), int(nz))
+
+    def get_table_s1r2(self, nrho=None, nz=None):
+        nrho, nz = (nrho, nz) if nrho else self.s1r2_shape
+        out = np.empty(2 * nrho * nz)
+        self._check(self.lib.steps_gpu_get_table_s1r2(_d(out)))
+        return out
+
+    def set_radial_table(self, tab):
+        tab = np.ascontiguousarray(tab, dtype=np.float64)
+        self._check(self.lib.steps_gpu_set_radial_table(int(tab.size), _d(tab)))
+
+    # tuning / instrumentation
+    def set_tuning(self, threads, ipt, jsplit=0):
+        self._check(self.lib.steps_gpu_set_tuning(int(threads), int(ipt), int(jsplit)))
+
+    def autotune(self, p: Params, id_min=0, id_max=None):
+        out = (C.c_int * 2)()
+        if id_max is None:
+            id_max = self.n - 1
+        self._check(self.lib.steps_gpu_autotune(C.byref(p), int(id_min), int(id_max), out))
+        return int(out[0]), int(out[1])
+
+    def launch_count(self) -> int:
+        return int(self.lib.steps_gpu_launch_count())
+
+    def phase_ms(self, phase: int) -> float:
+        return float(self.lib.steps_gpu_last_phase_ms(int(phase)))
+
+    def mark(self, slot: int):
+        self._check(self.lib.steps_gpu_timer_mark(int(slot)))
+
+    def elapsed_ms(self, a: int, b: int) -> float:
+        return float(self.lib.steps_gpu_timer_elapsed_ms(int(a), int(b)))
+
+    def flush_l2(self, nbytes: int = 512 << 20):
+        self._check(self.lib.steps_gpu_flush_l2(int(nbytes)))
+
+    def synchronize(self):
+        self._check(self.lib.steps_gpu_synchronize())
+
+    def measure_peaks(self):
+        f32 = C.c_double(0); f64 = C.c_double(0)
+        self._check(self.lib.steps_gpu_measure_peaks(C.byref(f32), C.byref(f64)))
+        return f32.value, f64.value

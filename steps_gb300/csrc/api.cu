@@ -1,0 +1,496 @@
+// The extern "C" entry points of libsteps_gb300 (declared in
+// include/steps_gb300.h) and the persistent single-GPU context behind them.
+//
+// The reference CUDA path allocates, uploads and frees every device buffer on
+// every force call and spreads the i range over an OpenMP team of GPUs
+// (StePS/src/forces_cuda.cu:933-1105). Here one context lives from
+// steps_gpu_init to steps_gpu_shutdown: masses, softening and tables are
+// uploaded once, positions once per call, and all work runs on one stream.
+#include <stdio.h>
+#include <string.h>
+
+#include <mutex>
+#include <string>
+
+#include "common.cuh"
+#include "context.cuh"
+
+namespace steps {
+
+static Ctx g_ctx;
+static thread_local std::string g_err;
+
+Ctx &ctx() { return g_ctx; }
+
+void fail(int code, const std::string &msg) { throw Error{code, msg}; }
+
+void check_cuda(cudaError_t e, const char *what, const char *file, int line)
+{
+    if (e == cudaSuccess) return;
+    char buf[512];
+    snprintf(buf, sizeof buf, "%s failed: %s (%s:%d)", what, cudaGetErrorString(e), file, line);
+    fail(e == cudaErrorMemoryAllocation ? STEPS_E_NOMEM : STEPS_E_CUDA, buf);
+}
+
+void note_launch(const char *name)
+{
+    g_ctx.launches++;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        char buf[256];
+        snprintf(buf, sizeof buf, "launch of %s failed: %s", name, cudaGetErrorString(e));
+        fail(STEPS_E_CUDA, buf);
+    }
+}
+
+void DevBuf::grow(size_t want)
+{
+    if (want <= bytes && p) return;
+    if (p) {
+        cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    size_t sz = want < 256 ? 256 : want;
+    cudaError_t e = cudaMalloc(&p, sz);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        p = nullptr;
+        char buf[160];
+        snprintf(buf, sizeof buf, "cudaMalloc of %zu bytes failed: %s", sz, cudaGetErrorString(e));
+        fail(STEPS_E_NOMEM, buf);
+    }
+    bytes = sz;
+}
+
+void DevBuf::release()
+{
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+}
+
+void require_init()
+{
+    if (g_ctx.device < 0) fail(STEPS_E_STATE, "steps_gpu_init has not been called");
+    STEPS_CUDA(cudaSetDevice(g_ctx.device));
+}
+
+KParams derive_params(const steps_params *p)
+{
+    if (!p) fail(STEPS_E_ARG, "params is NULL");
+    KParams k{};
+    k.topology = p->topology;
+    k.is_periodic = p->is_periodic;
+    k.s1r2_images = p->s1r2_images;
+    k.order = p->ewald_order;
+    k.L = p->L;
+    k.halfL = 0.5 * p->L;
+    k.rsim = p->rsim;
+    // ewald_max = IS_PERIODIC + 1, ewald_cut = ewald_max - 0.4 (StePS/src/main.cc:1270-1271,
+    // StePS/src/forces_cuda.cu:659-660).
+    k.emax = p->is_periodic + 1;
+    k.cutL = ((double)k.emax - 0.4) * p->L;
+    if (p->topology < STEPS_R3 || p->topology > STEPS_S1R2) fail(STEPS_E_ARG, "unknown topology");
+    if (p->topology != STEPS_R3) {
+        if (!(p->L > 0)) fail(STEPS_E_ARG, "periodic topology needs L > 0");
+        if (p->is_periodic < 1) fail(STEPS_E_ARG, "periodic topology needs IS_PERIODIC >= 1");
+    }
+    if (p->topology == STEPS_T3 && p->is_periodic >= 2 && p->ewald_order != 2 && p->ewald_order != 4)
+        fail(STEPS_E_ARG, "T3 interpolation order must be 2 or 4");
+    if (p->topology == STEPS_S1R2 && p->is_periodic >= 2 && !p->s1r2_images && p->ewald_order != 0 &&
+        p->ewald_order != 2 && p->ewald_order != 4)
+        fail(STEPS_E_ARG, "S1R2 table interpolation order must be 0, 2 or 4");
+    if (p->topology == STEPS_S1R2 && p->s1r2_images && k.emax > 64) fail(STEPS_E_ARG, "IS_PERIODIC too large");
+    if (p->cosmology == 1 && p->comoving == 1) {
+        k.comoving_bg = 1;
+        k.bg_coef = p->mass_in_unit_sphere;
+    } else if (p->cosmology == 1 && p->comoving == 0) {
+        k.comoving_bg = 2;
+        k.bg_coef = p->h0 * p->h0 * p->omega_lambda;
+    }
+    if (p->topology == STEPS_T3) k.comoving_bg = 0;  // T^3 has no background term
+    return k;
+}
+
+Tables device_tables(const KParams &kp)
+{
+    Ctx &c = g_ctx;
+    Tables t{};
+    t.t3 = c.t3.as<double>();
+    t.t3_ng = c.t3_ng;
+    t.s1r2 = c.s1r2.as<double>();
+    t.nrho = c.nrho;
+    t.nz = c.nz;
+    t.rho_max = 2.25 * kp.rsim;  // EWALD_LOOKUP_TABLE_RADIAL_EXTENT_FACTOR, StePS/src/global_variables.h:39
+    t.radial = c.radial.as<double>();
+    t.radial_size = c.radial_size;
+    if (kp.topology == STEPS_T3 && kp.is_periodic >= 2 && c.t3_ng <= 0)
+        fail(STEPS_E_STATE, "T3 Ewald run needs a table (steps_gpu_set_table_t3 / steps_gpu_build_table_t3)");
+    if (kp.topology == STEPS_S1R2 && kp.is_periodic >= 2 && !kp.s1r2_images && c.nrho <= 0)
+        fail(STEPS_E_STATE, "S1R2 table run needs a table (steps_gpu_set_table_s1r2 / steps_gpu_build_table_s1r2)");
+    if (kp.topology == STEPS_S1R2 && kp.is_periodic >= 2 && !kp.s1r2_images && c.nrho < 2)
+        fail(STEPS_E_TABLE, "S1R2 table needs at least 2 radial points");
+    return t;
+}
+
+void compute_forces(const steps_params *p, int precision, int id_min, int id_max, bool reuse_order)
+{
+    Ctx &c = g_ctx;
+    require_init();
+    if (c.n <= 0) fail(STEPS_E_STATE, "no particles: call steps_gpu_set_particles first");
+    if (!c.have_x) fail(STEPS_E_STATE, "no positions uploaded");
+    if (id_min < 0 || id_max >= c.n || id_max < id_min) fail(STEPS_E_ARG, "i range outside [0, n)");
+    if (precision != STEPS_FP64 && precision != STEPS_MIXED) fail(STEPS_E_ARG, "unknown precision mode");
+    KParams kp = derive_params(p);
+    Tables tb = device_tables(kp);
+    int ni = id_max - id_min + 1;
+    double *F = c.F.ensure<double>(3 * (size_t)c.n);
+    if (precision == STEPS_FP64)
+        forces_fp64(kp, tb, c.x.as<double>(), c.n, id_min, ni, F);
+    else
+        forces_mixed(kp, tb, c.x.as<double>(), c.n, id_min, ni, F, reuse_order);
+    c.F_lo = id_min;
+    c.F_ni = ni;
+    c.F_valid = id_min == 0 && ni == c.n;
+}
+
+}  // namespace steps
+
+using namespace steps;
+
+template <class Fn>
+static int guarded(Fn &&fn)
+{
+    try {
+        fn();
+        return STEPS_OK;
+    } catch (const Error &e) {
+        g_err = e.msg;
+        return e.code;
+    } catch (const std::exception &e) {
+        g_err = e.what();
+        return STEPS_E_STATE;
+    }
+}
+
+namespace steps {
+int run_guarded(void (*body)(void *), void *arg)
+{
+    return guarded([&] { body(arg); });
+}
+}  // namespace steps
+
+extern "C" {
+
+int steps_gpu_abi_version(void) { return STEPS_GB300_ABI_VERSION; }
+
+const char *steps_gpu_error_string(void) { return g_err.c_str(); }
+
+int steps_gpu_init(int device)
+{
+    return guarded([&] {
+        Ctx &c = g_ctx;
+        if (c.device == device) return;
+        if (c.device >= 0) fail(STEPS_E_STATE, "already initialised on another device; call steps_gpu_shutdown first");
+        int count = 0;
+        STEPS_CUDA(cudaGetDeviceCount(&count));
+        if (device < 0 || device >= count) fail(STEPS_E_ARG, "no such CUDA device");
+        STEPS_CUDA(cudaSetDevice(device));
+        STEPS_CUDA(cudaDeviceGetAttribute(&c.nsm, cudaDevAttrMultiProcessorCount, device));
+        STEPS_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+        for (auto &e : c.marks) STEPS_CUDA(cudaEventCreate(&e));
+        for (auto &e : c.phase) STEPS_CUDA(cudaEventCreate(&e));
+        c.device = device;
+        c.launches = 0;
+    });
+}
+
+int steps_gpu_shutdown(void)
+{
+    return guarded([&] {
+        Ctx &c = g_ctx;
+        if (c.device < 0) return;
+        cudaSetDevice(c.device);
+        cudaStreamSynchronize(c.stream);
+        batch_release();
+        DevBuf *bufs[] = {&c.m64, &c.eps64, &c.x, &c.v, &c.F, &c.pack64, &c.partial, &c.bbox, &c.counter,
+                          &c.status, &c.flush, &c.peaks, &c.t3, &c.s1r2, &c.radial};
+        for (DevBuf *b : bufs) b->release();
+        TileSet *ts[] = {&c.tj, &c.ti};
+        for (TileSet *t : ts) {
+            for (int k = 0; k < 2; k++) { t->keys[k].release(); t->vals[k].release(); }
+            t->hist.release(); t->pack.release(); t->eps.release(); t->meta.release();
+            *t = TileSet();
+        }
+        for (auto &e : c.marks) cudaEventDestroy(e);
+        for (auto &e : c.phase) cudaEventDestroy(e);
+        cudaStreamDestroy(c.stream);
+        g_ctx = Ctx();
+    });
+}
+
+int steps_gpu_set_particles(int n, const double *m, const double *eps)
+{
+    return guarded([&] {
+        require_init();
+        Ctx &c = g_ctx;
+        if (n <= 0 || !m || !eps) fail(STEPS_E_ARG, "set_particles: n must be > 0 and m, eps non-NULL");
+        if (n > (1 << 30)) fail(STEPS_E_ARG, "set_particles: n too large");
+        if (n != c.n) {
+            c.have_x = c.have_v = c.F_valid = false;
+            c.tj.ordered = c.ti.ordered = false;
+        }
+        STEPS_CUDA(cudaMemcpyAsync(c.m64.ensure<double>(n), m, sizeof(double) * n, cudaMemcpyHostToDevice, c.stream));
+        STEPS_CUDA(cudaMemcpyAsync(c.eps64.ensure<double>(n), eps, sizeof(double) * n, cudaMemcpyHostToDevice, c.stream));
+        STEPS_CUDA(cudaStreamSynchronize(c.stream));
+        c.n = n;
+    });
+}
+
+int steps_gpu_upload_positions(const double *x)
+{
+    return guarded([&] {
+        require_init();
+        Ctx &c = g_ctx;
+        if (c.n <= 0) fail(STEPS_E_STATE, "no particles: call steps_gpu_set_particles first");
+        if (!x) fail(STEPS_E_ARG, "x is NULL");
+        STEPS_CUDA(cudaMemcpyAsync(c.x.ensure<double>(3 * (size_t)c.n), x, sizeof(double) * 3 * c.n,
+                                   cudaMemcpyHostToDevice, c.stream));
+        c.have_x = true;
+        c.F_valid = false;
+    });
+}
+
+int steps_gpu_upload_velocities(const double *v)
+{
+    return guarded([&] {
+        require_init();
+        Ctx &c = g_ctx;
+        if (c.n <= 0) fail(STEPS_E_STATE, "no particles: call steps_gpu_set_particles first");
+        if (!v) fail(STEPS_E_ARG, "v is NULL");
+        STEPS_CUDA(cudaMemcpyAsync(c.v.ensure<double>(3 * (size_t)c.n), v, sizeof(double) * 3 * c.n,
+                                   cudaMemcpyHostToDevice, c.stream));
+        c.have_v = true;
+    });
+}
+
+int steps_gpu_forces_resident(const steps_params *p, int precision, int id_min, int id_max)
+{
+    return guarded([&] { compute_forces(p, precision, id_min, id_max, false); });
+}
+
+int steps_gpu_download_forces(double *F)
+{
+    return guarded([&] {
+        require_init();
+        Ctx &c = g_ctx;
+        if (!F) fail(STEPS_E_ARG, "F is NULL");
+        if (c.F_ni <= 0) fail(STEPS_E_STATE, "no forces computed");
+        STEPS_CUDA(cudaMemcpyAsync(F, c.F.as<double>(), sizeof(double) * 3 * c.F_ni, cudaMemcpyDeviceToHost, c.stream));
+        STEPS_CUDA(cudaStreamSynchronize(c.stream));
+    });
+}
+
+int steps_gpu_forces(const steps_params *p, int precision, const double *x, double *F, int id_min, int id_max)
+{
+    return guarded([&] {
+        require_init();
+        Ctx &c = g_ctx;
+        if (!x || !F) fail(STEPS_E_ARG, "x and F must be non-NULL");
+        if (c.n <= 0) fail(STEPS_E_STATE, "no particles: call steps_gpu_set_particles first");
+        STEPS_CUDA(cudaMemcpyAsync(c.x.ensure<double>(3 * (size_t)c.n), x, sizeof(double) * 3 * c.n,
+                                   cudaMemcpyHostToDevice, c.stream));
+        c.have_x = true;
+        compute_forces(p, precision, id_min, id_max, false);
+        int ni = id_max - id_min + 1;
+        STEPS_CUDA(cudaMemcpyAsync(F, c.F.as<double>(), sizeof(double) * 3 * (size_t)ni, cudaMemcpyDeviceToHost,
+                                   c.stream));
+        STEPS_CUDA(cudaStreamSynchronize(c.stream));
+    });
+}
+
+int steps_gpu_download_state(double *x, double *v, double *F)
+{
+    return guarded([&] {
+        require_init();
+        Ctx &c = g_ctx;
+        size_t b = sizeof(double) * 3 * (size_t)c.n;
+        if (x) {
+            if (!c.have_x) fail(STEPS_E_STATE, "no positions");
+            STEPS_CUDA(cudaMemcpyAsync(x, c.x.as<double>(), b, cudaMemcpyDeviceToHost, c.stream));
+        }
+        if (v) {
+            if (!c.have_v) fail(STEPS_E_STATE, "no velocities");
+            STEPS_CUDA(cudaMemcpyAsync(v, c.v.as<double>(), b, cudaMemcpyDeviceToHost, c.stream));
+        }
+        if (F) {
+            if (c.F_ni <= 0) fail(STEPS_E_STATE, "no forces computed");
+            STEPS_CUDA(cudaMemcpyAsync(F, c.F.as<double>(), sizeof(double) * 3 * c.F_ni, cudaMemcpyDeviceToHost,
+                                       c.stream));
+        }
+        STEPS_CUDA(cudaStreamSynchronize(c.stream));
+    });
+}
+
+int steps_gpu_set_table_t3(int ngrid, const double *table)
+{
+    return guarded([&] {
+        require_init();
+        Ctx &c = g_ctx;
+        if (ngrid < 2 || ngrid > 1024 || !table) fail(STEPS_E_ARG, "set_table_t3: ngrid in [2, 1024], table non-NULL");
+        size_t cnt = 3 * (size_t)ngrid * ngrid * ngrid;
+        STEPS_CUDA(cudaMemcpyAsync(c.t3.ensure<double>(cnt), table, cnt * sizeof(double), cudaMemcpyHostToDevice,
+                                   c.stream));
+        STEPS_CUDA(cudaStreamSynchronize(c.stream));
+        c.t3_ng = ngrid;
+    });
+}
+
+int steps_gpu_get_table_t3(double *out)
+{
+    return guarded([&] {
+        require_init();
+        Ctx &c = g_ctx;
+        if (!out) fail(STEPS_E_ARG, "out is NULL");
+        if (c.t3_ng <= 0) fail(STEPS_E_STATE, "no T3 table");
+        size_t cnt = 3 * (size_t)c.t3_ng * c.t3_ng * c.t3_ng;
+        STEPS_CUDA(cudaMemcpyAsync(out, c.t3.as<double>(), cnt * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        STEPS_CUDA(cudaStreamSynchronize(c.stream));
+    });
+}
+
+int steps_gpu_set_table_s1r2(int nrho, int nz, const double *table)
+{
+    return guarded([&] {
+        require_init();
+        Ctx &c = g_ctx;
+        if (nrho < 1 || nz < 1 || !table || (long long)nrho * nz > (1LL << 28))
+            fail(STEPS_E_ARG, "set_table_s1r2: bad shape or NULL table");
+        size_t cnt = 2 * (size_t)nrho * nz;
+        STEPS_CUDA(cudaMemcpyAsync(c.s1r2.ensure<double>(cnt), table, cnt * sizeof(double), cudaMemcpyHostToDevice,
+                                   c.stream));
+        STEPS_CUDA(cudaStreamSynchronize(c.stream));
+        c.nrho = nrho;
+        c.nz = nz;
+    });
+}
+
+int steps_gpu_get_table_s1r2(double *out)
+{
+    return guarded([&] {
+        require_init();
+        Ctx &c = g_ctx;
+        if (!out) fail(STEPS_E_ARG, "out is NULL");
+        if (c.nrho <= 0) fail(STEPS_E_STATE, "no S1R2 table");
+        size_t cnt = 2 * (size_t)c.nrho * c.nz;
+        STEPS_CUDA(cudaMemcpyAsync(out, c.s1r2.as<double>(), cnt * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        STEPS_CUDA(cudaStreamSynchronize(c.stream));
+    });
+}
+
+int steps_gpu_set_radial_table(int size, const double *table)
+{
+    return guarded([&] {
+        require_init();
+        Ctx &c = g_ctx;
+        if (size < 2 || !table) fail(STEPS_E_ARG, "set_radial_table: size >= 2 and table non-NULL");
+        STEPS_CUDA(cudaMemcpyAsync(c.radial.ensure<double>(size), table, size * sizeof(double), cudaMemcpyHostToDevice,
+                                   c.stream));
+        STEPS_CUDA(cudaStreamSynchronize(c.stream));
+        c.radial_size = size;
+    });
+}
+
+int steps_gpu_set_tuning(int threads, int ipt, int jsplit)
+{
+    return guarded([&] {
+        if (!shape_supported(threads, ipt)) fail(STEPS_E_ARG, "unsupported kernel shape");
+        if (jsplit < 0) fail(STEPS_E_ARG, "jsplit must be >= 0");
+        g_ctx.shape.threads = threads;
+        g_ctx.shape.ipt = ipt;
+        g_ctx.shape.jsplit = jsplit;
+        g_ctx.shape_fixed = true;
+    });
+}
+
+int steps_gpu_autotune(const steps_params *p, int id_min, int id_max, int *out)
+{
+    return guarded([&] {
+        require_init();
+        Ctx &c = g_ctx;
+        static const int shapes[][2] = {{64, 2}, {64, 4}, {128, 1}, {128, 2}, {128, 4}, {256, 1}, {256, 2}};
+        Shape keep = c.shape;
+        float best = 1e30f;
+        Shape bestS = keep;
+        for (auto &s : shapes) {
+            c.shape.threads = s[0];
+            c.shape.ipt = s[1];
+            c.shape.jsplit = 0;
+            compute_forces(p, STEPS_MIXED, id_min, id_max, false);  // warm
+            compute_forces(p, STEPS_MIXED, id_min, id_max, true);
+            STEPS_CUDA(cudaEventSynchronize(c.phase[2]));
+            float ms = 0;
+            STEPS_CUDA(cudaEventElapsedTime(&ms, c.phase[1], c.phase[2]));
+            if (ms < best) { best = ms; bestS = c.shape; }
+        }
+        c.shape = bestS;
+        c.shape_fixed = true;
+        if (out) { out[0] = bestS.threads; out[1] = bestS.ipt; }
+    });
+}
+
+long long steps_gpu_launch_count(void) { return g_ctx.launches; }
+
+double steps_gpu_last_phase_ms(int phase)
+{
+    Ctx &c = g_ctx;
+    if (c.device < 0 || !c.phase_valid || phase < 0 || phase > 2) return -1.0;
+    if (cudaEventSynchronize(c.phase[phase + 1]) != cudaSuccess) return -1.0;
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, c.phase[phase], c.phase[phase + 1]) != cudaSuccess) return -1.0;
+    return ms;
+}
+
+double steps_gpu_last_pairs(void) { return g_ctx.last_pairs; }
+
+int steps_gpu_timer_mark(int slot)
+{
+    return guarded([&] {
+        require_init();
+        if (slot < 0 || slot >= 16) fail(STEPS_E_ARG, "timer slot must be in [0, 16)");
+        STEPS_CUDA(cudaEventRecord(g_ctx.marks[slot], g_ctx.stream));
+        g_ctx.mark_set[slot] = true;
+    });
+}
+
+double steps_gpu_timer_elapsed_ms(int a, int b)
+{
+    Ctx &c = g_ctx;
+    if (c.device < 0 || a < 0 || b < 0 || a >= 16 || b >= 16 || !c.mark_set[a] || !c.mark_set[b]) return -1.0;
+    if (cudaEventSynchronize(c.marks[b]) != cudaSuccess) return -1.0;
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, c.marks[a], c.marks[b]) != cudaSuccess) return -1.0;
+    return ms;
+}
+
+int steps_gpu_flush_l2(long long bytes)
+{
+    return guarded([&] {
+        require_init();
+        if (bytes <= 0 || bytes > (8LL << 30)) fail(STEPS_E_ARG, "flush size out of range");
+        void *p = g_ctx.flush.ensure<char>((size_t)bytes);
+        STEPS_CUDA(cudaMemsetAsync(p, (int)(g_ctx.launches & 0xff), (size_t)bytes, g_ctx.stream));
+    });
+}
+
+int steps_gpu_synchronize(void)
+{
+    return guarded([&] {
+        require_init();
+        STEPS_CUDA(cudaStreamSynchronize(g_ctx.stream));
+        STEPS_CUDA(cudaGetLastError());
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,168 @@
+// Shared declarations of libsteps_gb300: the persistent device context,
+// error handling, kernel parameter blocks and device math helpers.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "steps_gb300.h"
+
+namespace steps {
+
+// ---------------------------------------------------------------- errors --
+
+struct Error {
+    int code;
+    std::string msg;
+};
+
+[[noreturn]] void fail(int code, const std::string &msg);
+void check_cuda(cudaError_t e, const char *what, const char *file, int line);
+#define STEPS_CUDA(expr) ::steps::check_cuda((expr), #expr, __FILE__, __LINE__)
+
+// ------------------------------------------------------------ device buf --
+
+// A growable device allocation owned by the context. Grows (free + malloc)
+// only when a request exceeds its capacity; never shrinks until shutdown.
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    template <class T>
+    T *as() const { return static_cast<T *>(p); }
+    template <class T>
+    T *ensure(size_t count) { grow(count * sizeof(T)); return static_cast<T *>(p); }
+    void grow(size_t want);
+    void release();
+};
+
+// ------------------------------------------------- kernel parameter blocks --
+
+// Physics parameters as the kernels read them (derived once per call).
+struct KParams {
+    int topology;
+    int is_periodic;
+    int comoving_bg;   // 0 none, 1 mass_in_unit_sphere * x, 2 H0^2 Omega_L * x
+    int s1r2_images;   // S1R2 with is_periodic >= 2: explicit images (1) or table (0)
+    int emax;          // S1R2 image range [-emax, emax] (ewald_max = IS_PERIODIC + 1)
+    int order;         // interpolation order of the active table
+    double L, halfL, cutL;  // cutL = (emax - 0.4) * L
+    double bg_coef;
+    double rsim;
+};
+
+// Tables resident on the device (FP64 as StePS builds them).
+struct Tables {
+    const double *t3;  // ngrid^3 * 3
+    int t3_ng;
+    const double *s1r2;  // nrho * nz * 2
+    int nrho, nz;
+    double rho_max;
+    const double *radial;  // cylindrical background multiplier
+    int radial_size;
+};
+
+// A set of particles ordered along a Morton curve and cut into tiles of T.
+// pack[q] = (x - c, y - c, z - c, m) of the q-th particle in curve order,
+// relative to its tile's centre c (exactly representable in FP32);
+// meta[2t] = (c.x, c.y, c.z, eps_max), meta[2t+1] = (half extents, 0).
+struct TileSet {
+    int lo = 0, count = 0;  // original index range [lo, lo + count)
+    int T = 0, ntiles = 0;
+    DevBuf keys[2], vals[2], hist;
+    DevBuf pack, eps, meta;
+    int perm_sel = 0;  // vals[perm_sel] holds curve position -> original index
+    bool ordered = false;
+    const uint32_t *perm() const { return vals[perm_sel].as<uint32_t>(); }
+};
+
+// Mixed-kernel launch shape.
+struct Shape {
+    int threads = 128;
+    int ipt = 2;
+    int jsplit = 0;
+};
+
+// ------------------------------------------------------------- utilities --
+
+inline __host__ __device__ int div_up(int a, int b) { return (a + b - 1) / b; }
+
+// Kernel-launch bookkeeping: counts launches and surfaces launch errors.
+void note_launch(const char *name);
+
+// ---------------------------------------------------- device math helpers --
+
+// MUFU reciprocal square root, approximate (relative error < 2^-22), FTZ.
+__device__ __forceinline__ float rsqrt_mufu(float x)
+{
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+__device__ __forceinline__ float sqrt_mufu(float x)
+{
+    float y;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+__device__ __forceinline__ float rcp_mufu(float x)
+{
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// FP64 1/sqrt(x) for 1e-36 < x < 1e36: a single-precision MUFU seed (relative
+// error e0 < 2^-22) refined by one third-order Householder step of Newton's
+// iteration for f(y) = y^-2 - x, i.e. the binomial series of (1 - e)^(-1/2):
+//   e = 1 - x y^2,  y' = y (1 + e/2 + 3 e^2 / 8),  error O(e0^3) < 1e-19,
+// so the result is within a couple of ulp of 1/sqrt(x).
+__device__ __forceinline__ double rsqrt_fp64(double x)
+{
+    double y = (double)rsqrt_mufu(__double2float_rn(x));
+    double t = x * y;
+    double e = fma(-t, y, 1.0);
+    double p = fma(0.375, e, 0.5);
+    return fma(y * e, p, y);
+}
+
+// Cubic-spline softened force coefficient w(r, beta) for r < beta (the
+// r >= beta branch is 1/r^3). StePS/src/forces.cc:52-87,
+// StePS/src/forces_cuda.cu:466-519, written in u = r / beta:
+//   u <= 1/2 : (32 u^3 - 38.4 u^2 + 32/3) / beta^3
+//   u >  1/2 : (-32/3 u^3 + 38.4 u^2 - 48 u + 64/3) / beta^3 - (1/15) / r^3
+__device__ __forceinline__ double spline_inner_fp64(double r, double beta)
+{
+    double ib = 1.0 / beta;
+    double u = r * ib;
+    double ib3 = ib * ib * ib;
+    if (u <= 0.5) return ib3 * (u * u * (32.0 * u - 38.4) + 32.0 / 3.0);
+    double r3 = r * r * r;
+    return ib3 * (u * (u * (-32.0 / 3.0 * u + 38.4) - 48.0) + 64.0 / 3.0) - (1.0 / 15.0) / r3;
+}
+
+__device__ __forceinline__ double softening_fp64(double r2, double beta)
+{
+    if (r2 >= beta * beta) {
+        double y = rsqrt_fp64(r2);
+        return y * y * y;
+    }
+    return spline_inner_fp64(sqrt(r2), beta);
+}
+
+__device__ __forceinline__ float spline_inner_f32(float r2, float beta)
+{
+    float r = sqrt_mufu(r2);
+    float ib = rcp_mufu(beta);
+    float u = r * ib;
+    float ib3 = ib * ib * ib;
+    if (u <= 0.5f) return ib3 * (u * u * (32.0f * u - 38.4f) + (32.0f / 3.0f));
+    float ir = rcp_mufu(r);
+    return ib3 * (u * (u * (-32.0f / 3.0f * u + 38.4f) - 48.0f) + (64.0f / 3.0f)) -
+           (1.0f / 15.0f) * ir * ir * ir;
+}
+
+}  // namespace steps

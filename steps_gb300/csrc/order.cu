@@ -1,0 +1,339 @@
+// Spatial ordering of a particle set for the mixed-precision kernels:
+//   1. bounding box (FP64, atomic min/max on order-preserving integer images),
+//   2. 63-bit Morton keys (21 bits per axis) of the positions in the box,
+//   3. a stable least-significant-digit radix sort of (key, index) pairs,
+//   4. tiles of T consecutive particles along the curve: each tile gets an
+//      FP32-exact centre c, FP32 offsets x - c computed in FP64, half extents
+//      and its largest softening length.
+// The order only sets locality (tile size, hence FP32 offset magnitude and
+// the near/far split); the forces do not depend on it beyond rounding.
+#include "common.cuh"
+#include "context.cuh"
+
+namespace steps {
+
+namespace {
+
+constexpr int SORT_THREADS = 256;
+constexpr int SORT_ITEMS = 8;  // elements per thread per block
+constexpr int SORT_TILE = SORT_THREADS * SORT_ITEMS;
+constexpr int RADIX_BITS = 8;
+constexpr int RADIX = 1 << RADIX_BITS;
+
+__device__ __forceinline__ unsigned long long ordered_bits(double d)
+{
+    unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+}
+
+__device__ __forceinline__ double from_ordered_bits(unsigned long long u)
+{
+    unsigned long long b = (u & 0x8000000000000000ull) ? (u & 0x7fffffffffffffffull) : ~u;
+    return __longlong_as_double((long long)b);
+}
+
+__global__ void k_bbox_init(unsigned long long *bb)
+{
+    int t = threadIdx.x;
+    if (t < 3) bb[t] = ~0ull;        // min
+    else if (t < 6) bb[t] = 0ull;    // max
+}
+
+__global__ void k_bbox(const double *__restrict__ x, int lo, int count, unsigned long long *bb)
+{
+    double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300};
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < count; q += gridDim.x * blockDim.x) {
+        const double *p = x + 3 * (size_t)(lo + q);
+        for (int k = 0; k < 3; k++) { mn[k] = fmin(mn[k], p[k]); mx[k] = fmax(mx[k], p[k]); }
+    }
+    for (int k = 0; k < 3; k++)
+        for (int o = 16; o > 0; o >>= 1) {
+            mn[k] = fmin(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], o));
+            mx[k] = fmax(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], o));
+        }
+    if ((threadIdx.x & 31) == 0)
+        for (int k = 0; k < 3; k++) {
+            atomicMin(&bb[k], ordered_bits(mn[k]));
+            atomicMax(&bb[3 + k], ordered_bits(mx[k]));
+        }
+}
+
+__device__ __forceinline__ unsigned long long spread3(unsigned long long v)
+{
+    // Spread the low 21 bits of v to every third bit.
+    v &= 0x1fffffull;
+    v = (v | (v << 32)) & 0x1f00000000ffffull;
+    v = (v | (v << 16)) & 0x1f0000ff0000ffull;
+    v = (v | (v << 8)) & 0x100f00f00f00f00full;
+    v = (v | (v << 4)) & 0x10c30c30c30c30c3ull;
+    v = (v | (v << 2)) & 0x1249249249249249ull;
+    return v;
+}
+
+// Keys for particles lo..lo+count-1; prefix (the realisation index of a batch)
+// occupies the bits above 3*bits.
+__global__ void k_keys(const double *__restrict__ x, int lo, int count, const unsigned long long *bb, int bits,
+                       unsigned long long prefix, unsigned long long *keys, uint32_t *vals)
+{
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= count) return;
+    double cells = (double)(1u << bits);
+    const double *p = x + 3 * (size_t)(lo + q);
+    unsigned long long key = 0;
+    for (int k = 0; k < 3; k++) {
+        double lo_k = from_ordered_bits(bb[k]);
+        double hi_k = from_ordered_bits(bb[3 + k]);
+        double span = hi_k - lo_k;
+        double u = span > 0 ? (p[k] - lo_k) / span * cells : 0.0;
+        long long c = (long long)u;
+        c = c < 0 ? 0 : (c >= (long long)cells ? (long long)cells - 1 : c);
+        key |= spread3((unsigned long long)c) << k;
+    }
+    keys[q] = key | (prefix << (3 * bits));
+    vals[q] = (uint32_t)(lo + q);
+}
+
+// Per-block digit histograms, stored digit-major: hist[d * nblk + b].
+__global__ void __launch_bounds__(SORT_THREADS) k_hist(const unsigned long long *__restrict__ keys, int n, int shift,
+                                                      uint32_t *hist)
+{
+    __shared__ uint32_t h[RADIX];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    int base = blockIdx.x * SORT_TILE;
+    for (int r = 0; r < SORT_ITEMS; r++) {
+        int q = base + r * SORT_THREADS + threadIdx.x;
+        if (q < n) atomicAdd(&h[(keys[q] >> shift) & (RADIX - 1)], 1u);
+    }
+    __syncthreads();
+    hist[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = h[threadIdx.x];
+}
+
+// Exclusive scan of hist[0..total) in one block of 1024 threads.
+__global__ void __launch_bounds__(1024) k_scan(uint32_t *hist, int total)
+{
+    __shared__ uint32_t part[1024];
+    int t = threadIdx.x;
+    int per = div_up(total, 1024);
+    int b = t * per, e = min(total, b + per);
+    uint32_t s = 0;
+    for (int i = b; i < e; i++) s += hist[i];
+    part[t] = s;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        uint32_t v = t >= o ? part[t - o] : 0;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    uint32_t run = t ? part[t - 1] : 0;
+    for (int i = b; i < e; i++) {
+        uint32_t v = hist[i];
+        hist[i] = run;
+        run += v;
+    }
+}
+
+// Stable scatter: element order inside a block is (round, warp, lane), which is
+// the input order, and ranks among equal digits follow that order.
+__global__ void __launch_bounds__(SORT_THREADS) k_scatter(const unsigned long long *__restrict__ kin,
+                                                         const uint32_t *__restrict__ vin, int n, int shift,
+                                                         const uint32_t *__restrict__ hist,
+                                                         unsigned long long *__restrict__ kout,
+                                                         uint32_t *__restrict__ vout)
+{
+    constexpr int WARPS = SORT_THREADS / 32;
+    __shared__ uint32_t wc[WARPS][RADIX];
+    int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    uint32_t run = hist[(size_t)t * gridDim.x + blockIdx.x];  // thread t owns digit t
+    unsigned lt = (1u << lane) - 1u;
+    int base = blockIdx.x * SORT_TILE;
+    for (int r = 0; r < SORT_ITEMS; r++) {
+        for (int k = 0; k < WARPS; k++) wc[k][t] = 0;
+        __syncthreads();
+        int q = base + r * SORT_THREADS + t;
+        bool valid = q < n;
+        unsigned long long key = valid ? kin[q] : 0ull;
+        uint32_t val = valid ? vin[q] : 0u;
+        int d = valid ? (int)((key >> shift) & (RADIX - 1)) : RADIX;  // invalid lanes form their own group
+        unsigned peers = __match_any_sync(0xffffffffu, d);
+        int rank = __popc(peers & lt);
+        int leader = __ffs(peers) - 1;
+        if (valid && lane == leader) wc[w][d] = __popc(peers);
+        __syncthreads();
+        // Per digit: exclusive prefix over warps, continuing from earlier rounds.
+        for (int k = 0; k < WARPS; k++) {
+            uint32_t c = wc[k][t];
+            wc[k][t] = run;
+            run += c;
+        }
+        __syncthreads();
+        if (valid) {
+            uint32_t pos = wc[w][d] + rank;
+            kout[pos] = key;
+            vout[pos] = val;
+        }
+        __syncthreads();
+    }
+}
+
+__device__ __forceinline__ double warp_min(double v)
+{
+    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ double warp_max(double v)
+{
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+constexpr int TB_THREADS = 256;
+
+// One block per tile of T particles in curve order.
+__global__ void __launch_bounds__(TB_THREADS) k_tile_build(const double *__restrict__ x, const double *__restrict__ m,
+                                                          const double *__restrict__ eps,
+                                                          const uint32_t *__restrict__ perm, int count, int T,
+                                                          float4 *__restrict__ pack, float *__restrict__ epsf,
+                                                          float4 *__restrict__ meta)
+{
+    __shared__ double red[7][TB_THREADS / 32];
+    __shared__ float s_c[3];
+    int tile = blockIdx.x;
+    int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300}, em = 0.0;
+    for (int e = t; e < T; e += TB_THREADS) {
+        int q = tile * T + e;
+        if (q < count) {
+            uint32_t o = perm[q];
+            for (int k = 0; k < 3; k++) {
+                double v = x[3 * (size_t)o + k];
+                mn[k] = fmin(mn[k], v);
+                mx[k] = fmax(mx[k], v);
+            }
+            em = fmax(em, eps[o]);
+        }
+    }
+    for (int k = 0; k < 3; k++) { mn[k] = warp_min(mn[k]); mx[k] = warp_max(mx[k]); }
+    em = warp_max(em);
+    if (lane == 0) {
+        for (int k = 0; k < 3; k++) { red[k][w] = mn[k]; red[3 + k][w] = mx[k]; }
+        red[6][w] = em;
+    }
+    __syncthreads();
+    if (t == 0) {
+        double a[7];
+        for (int k = 0; k < 7; k++) a[k] = red[k][0];
+        for (int v = 1; v < TB_THREADS / 32; v++) {
+            for (int k = 0; k < 3; k++) { a[k] = fmin(a[k], red[k][v]); a[3 + k] = fmax(a[3 + k], red[3 + k][v]); }
+            a[6] = fmax(a[6], red[6][v]);
+        }
+        float c[3], h[3];
+        for (int k = 0; k < 3; k++) {
+            if (a[k] > a[3 + k]) { a[k] = 0.0; a[3 + k] = 0.0; }  // empty tile
+            c[k] = __double2float_rn(0.5 * (a[k] + a[3 + k]));
+            double ext = fmax(a[3 + k] - (double)c[k], (double)c[k] - a[k]);
+            // Round up so the FP32 half extent bounds every FP32 offset.
+            h[k] = __double2float_ru(ext * (1.0 + 1e-6)) + 1e-30f;
+            s_c[k] = c[k];
+        }
+        meta[2 * tile] = make_float4(c[0], c[1], c[2], __double2float_ru(a[6]));
+        meta[2 * tile + 1] = make_float4(h[0], h[1], h[2], 0.0f);
+    }
+    __syncthreads();
+    double cx = s_c[0], cy = s_c[1], cz = s_c[2];
+    for (int e = t; e < T; e += TB_THREADS) {
+        int q = tile * T + e;
+        if (q < count) {
+            uint32_t o = perm[q];
+            const double *p = x + 3 * (size_t)o;
+            pack[q] = make_float4(__double2float_rn(p[0] - cx), __double2float_rn(p[1] - cy),
+                                  __double2float_rn(p[2] - cz), __double2float_rn(m[o]));
+            epsf[q] = __double2float_rn(eps[o]);
+        } else {
+            pack[q] = make_float4(0.f, 0.f, 0.f, 0.f);  // massless padding at the tile centre
+            epsf[q] = 0.f;
+        }
+    }
+}
+
+}  // namespace
+
+void sort_pairs(TileSet &ts, int n, cudaStream_t st)
+{
+    int nblk = div_up(n, SORT_TILE);
+    uint32_t *hist = ts.hist.ensure<uint32_t>((size_t)RADIX * (nblk > 0 ? nblk : 1));
+    int cur = 0;
+    for (int shift = 0; shift < 64; shift += RADIX_BITS) {
+        k_hist<<<nblk, SORT_THREADS, 0, st>>>(ts.keys[cur].as<unsigned long long>(), n, shift, hist);
+        note_launch("k_hist");
+        k_scan<<<1, 1024, 0, st>>>(hist, RADIX * nblk);
+        note_launch("k_scan");
+        k_scatter<<<nblk, SORT_THREADS, 0, st>>>(ts.keys[cur].as<unsigned long long>(), ts.vals[cur].as<uint32_t>(), n,
+                                                 shift, hist, ts.keys[cur ^ 1].as<unsigned long long>(),
+                                                 ts.vals[cur ^ 1].as<uint32_t>());
+        note_launch("k_scatter");
+        cur ^= 1;
+    }
+    ts.perm_sel = cur;
+}
+
+// Orders particles [lo, lo+count) of the AoS FP64 array x along a Morton curve
+// (unless reuse is set and an order already exists) and (re)builds the tiles.
+void build_tiles(TileSet &ts, const double *x, const double *m64, const double *eps64, int lo, int count, int T,
+                 bool reuse, cudaStream_t st, unsigned long long *bbox_scratch)
+{
+    if (count <= 0) fail(STEPS_E_ARG, "empty particle set");
+    bool same = ts.ordered && ts.lo == lo && ts.count == count;
+    ts.T = T;
+    ts.ntiles = div_up(count, T);
+    size_t padded = (size_t)ts.ntiles * T;
+    if (!(reuse && same)) {
+        for (int b = 0; b < 2; b++) {
+            ts.keys[b].ensure<unsigned long long>(count);
+            ts.vals[b].ensure<uint32_t>(count);
+        }
+        k_bbox_init<<<1, 32, 0, st>>>(bbox_scratch);
+        note_launch("k_bbox_init");
+        int g = div_up(count, 256);
+        k_bbox<<<g < 1024 ? g : 1024, 256, 0, st>>>(x, lo, count, bbox_scratch);
+        note_launch("k_bbox");
+        k_keys<<<div_up(count, 256), 256, 0, st>>>(x, lo, count, bbox_scratch, 21, 0ull, ts.keys[0].as<unsigned long long>(),
+                                                  ts.vals[0].as<uint32_t>());
+        note_launch("k_keys");
+        sort_pairs(ts, count, st);
+        ts.lo = lo;
+        ts.count = count;
+        ts.ordered = true;
+    }
+    ts.pack.ensure<float4>(padded);
+    ts.eps.ensure<float>(padded);
+    ts.meta.ensure<float4>(2 * (size_t)ts.ntiles);
+    k_tile_build<<<ts.ntiles, TB_THREADS, 0, st>>>(x, m64, eps64, ts.perm(), count, T, ts.pack.as<float4>(),
+                                                   ts.eps.as<float>(), ts.meta.as<float4>());
+    note_launch("k_tile_build");
+}
+
+// Batched variant: keys carry the realisation index above the Morton bits, so
+// one sort orders every realisation's particles contiguously by realisation.
+void batch_keys(const double *x, int lo, int count, unsigned long long prefix, unsigned long long *keys, uint32_t *vals,
+                unsigned long long *bbox_scratch, cudaStream_t st)
+{
+    k_bbox_init<<<1, 32, 0, st>>>(bbox_scratch);
+    note_launch("k_bbox_init");
+    int g = div_up(count, 256);
+    k_bbox<<<g < 1024 ? g : 1024, 256, 0, st>>>(x, lo, count, bbox_scratch);
+    note_launch("k_bbox");
+    k_keys<<<div_up(count, 256), 256, 0, st>>>(x, lo, count, bbox_scratch, 19, prefix, keys, vals);
+    note_launch("k_keys");
+}
+
+void tile_build_range(const double *x, const double *m64, const double *eps64, const uint32_t *perm, int count, int T,
+                      float4 *pack, float *epsf, float4 *meta, cudaStream_t st)
+{
+    int nt = div_up(count, T);
+    k_tile_build<<<nt, TB_THREADS, 0, st>>>(x, m64, eps64, perm, count, T, pack, epsf, meta);
+    note_launch("k_tile_build");
+}
+
+}  // namespace steps

@@ -1,0 +1,423 @@
+// Mixed-precision direct-summation kernels: FP32 pair arithmetic on
+// tile-centred coordinates, FP64 accumulation per i particle.
+//
+// Layout (built by order.cu): particles sorted along a Morton curve and cut
+// into tiles of T = threads * ipt. Each particle is stored as an FP32 offset
+// from its tile's centre c (c exactly representable in FP32, the offset
+// computed in FP64 then rounded), so an FP32 offset carries ~1e-7 of the
+// tile's extent, not of the box.
+//
+// Work item = (i tile I, j chunk): a persistent block takes items from an
+// atomic counter, holds its T i particles in registers (ipt per thread) and
+// streams the chunk's j tiles through a double-buffered shared-memory ring
+// filled by cp.async. For a tile pair the block forms d_O = c_J - c_I in FP32
+// (one rounding), moves its i particles into J's frame (x_i - d_O) and then
+// every pair is d = x_j - (x_i - d_O): no FP64 operation per pair and none per
+// (i, J) beyond one FP32 subtraction. Per tile pair the FP32 sums are folded
+// into FP64 accumulators; partial sums per j chunk go to an FP64 buffer that
+// a reduction adds in chunk order (deterministic, no atomics on forces).
+//
+// Per tile pair the block classifies, from the tiles' boxes and largest
+// softening lengths, whether any pair can be closer than its softening
+// support beta = eps_i + eps_j (StePS/src/forces.cc:540). Far tile pairs run
+// the plain 1/r^3 loop (3 FADD, 3 FMUL/FFMA for r^2, 1 MUFU rsqrt, 3 FMUL,
+// 3 FFMA per pair); near ones run the full spline (forces.cc:52-87).
+#include "common.cuh"
+#include "context.cuh"
+
+namespace steps {
+
+namespace {
+
+enum Kind { K_R3 = 0, K_S1_IMG = 1, K_S1_GEN = 2 };
+
+struct MixedArgs {
+    const float4 *jpack;
+    const float *jeps;
+    const float4 *jmeta;
+    int njt;
+    const float4 *ipack;
+    const float *ieps;
+    const float4 *imeta;
+    int nit;
+    int S, tpc;  // j chunks per i tile, j tiles per chunk
+    int nitems;
+    unsigned *counter;
+    double *part;       // [S][nit*T][3]
+    size_t part_stride; // nit*T*3
+    float L, halfL, cutL;
+    int emax;
+    int nearest;        // S1R2 IS_PERIODIC == 1: nearest image along z only
+};
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+{
+    unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem)
+{
+    unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem));
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+template <int BLOCK, int IPT>
+__device__ __forceinline__ void stage_tile(const MixedArgs &a, int J, float4 *sp, float *se)
+{
+    constexpr int T = BLOCK * IPT;
+#pragma unroll
+    for (int k = 0; k < IPT; k++) {
+        int e = k * BLOCK + threadIdx.x;
+        size_t q = (size_t)J * T + e;
+        cp_async16(sp + e, a.jpack + q);
+        cp_async4(se + e, a.jeps + q);
+    }
+    cp_commit();
+}
+
+// Lower bound of |d| over the separations of two boxes along one axis.
+__device__ __forceinline__ float axis_gap(float dO, float hI, float hJ) { return fmaxf(fabsf(dO) - hI - hJ, 0.0f); }
+
+template <int KIND, int BLOCK, int IPT, int EMAX>
+__global__ void __launch_bounds__(BLOCK) k_pair_mixed(MixedArgs a)
+{
+    constexpr int T = BLOCK * IPT;
+    constexpr int NIMG = KIND == K_S1_IMG ? 2 * EMAX + 1 : 1;
+    __shared__ __align__(16) float4 sp[2][T];
+    __shared__ __align__(16) float se[2][T];
+    __shared__ int s_item;
+    const int tid = threadIdx.x;
+
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) s_item = (int)atomicAdd(a.counter, 1u);
+        __syncthreads();
+        const int item = s_item;
+        if (item >= a.nitems) return;
+        const int I = item / a.S;
+        const int chunk = item - I * a.S;
+        const int J0 = chunk * a.tpc;
+        const int J1 = min(a.njt, J0 + a.tpc);
+
+        const float4 mI0 = __ldg(a.imeta + 2 * I);
+        const float4 mI1 = __ldg(a.imeta + 2 * I + 1);
+        float xi[IPT], yi[IPT], zi[IPT], ei[IPT];
+        double ax[IPT], ay[IPT], az[IPT];
+#pragma unroll
+        for (int k = 0; k < IPT; k++) {
+            size_t q = (size_t)I * T + k * BLOCK + tid;
+            float4 p = __ldg(a.ipack + q);
+            xi[k] = p.x;
+            yi[k] = p.y;
+            zi[k] = p.z;
+            ei[k] = __ldg(a.ieps + q);
+            ax[k] = ay[k] = az[k] = 0.0;
+        }
+
+        if (J0 < J1) stage_tile<BLOCK, IPT>(a, J0, sp[0], se[0]);
+        for (int J = J0; J < J1; ++J) {
+            const int buf = (J - J0) & 1;
+            if (J + 1 < J1) {
+                stage_tile<BLOCK, IPT>(a, J + 1, sp[buf ^ 1], se[buf ^ 1]);
+                cp_wait<1>();
+            } else {
+                cp_wait<0>();
+            }
+            __syncthreads();
+
+            const float4 mJ0 = __ldg(a.jmeta + 2 * J);
+            const float4 mJ1 = __ldg(a.jmeta + 2 * J + 1);
+            const float dOx = mJ0.x - mI0.x, dOy = mJ0.y - mI0.y, dOz = mJ0.z - mI0.z;
+            const float bmax = mI0.w + mJ0.w;
+            const float bmax2 = bmax * bmax * 1.0001f + 1e-30f;
+            const float gx = axis_gap(dOx, mI1.x, mJ1.x), gy = axis_gap(dOy, mI1.y, mJ1.y);
+
+            bool full;  // near-field / mixed-cut tile pair: run every test per pair
+            float off[NIMG];
+            if (KIND == K_R3) {
+                const float gz = axis_gap(dOz, mI1.z, mJ1.z);
+                full = gx * gx + gy * gy + gz * gz <= bmax2;
+            } else if (KIND == K_S1_IMG) {
+                // Range of dz over the tile pair, then per image m: entirely
+                // inside the cut (offset m L), entirely outside (offset 1e18,
+                // whose 1/r^3 underflows to 0), or straddling (full path).
+                const float hz = mI1.z + mJ1.z;
+                const float lo = dOz - hz, hi = dOz + hz;
+                const float g2xy = gx * gx + gy * gy;
+                bool mixed = false, near = false;
+                const float cin = a.cutL * (1.0f - 1e-6f), cout = a.cutL * (1.0f + 1e-6f);
+#pragma unroll
+                for (int m = 0; m < NIMG; m++) {
+                    const float sh = (float)(m - EMAX) * a.L;
+                    const float l = lo + sh, h = hi + sh;
+                    const bool in = fmaxf(fabsf(l), fabsf(h)) <= cin;
+                    const bool out = l > cout || h < -cout;
+                    mixed |= !(in || out);
+                    off[m] = in ? sh : 1e18f;
+                    const float gz = (l <= 0.0f && h >= 0.0f) ? 0.0f : fminf(fabsf(l), fabsf(h));
+                    near |= !out && (g2xy + gz * gz <= bmax2);
+                }
+                full = mixed || near;
+            } else {
+                full = true;
+            }
+
+            float px[IPT], py[IPT], pz[IPT], fx[IPT], fy[IPT], fz[IPT];
+#pragma unroll
+            for (int k = 0; k < IPT; k++) {
+                px[k] = xi[k] - dOx;
+                py[k] = yi[k] - dOy;
+                pz[k] = zi[k] - dOz;
+                fx[k] = fy[k] = fz[k] = 0.0f;
+            }
+            const float4 *spb = sp[buf];
+            const float *seb = se[buf];
+
+            if (!full) {
+                if (KIND == K_R3) {
+#pragma unroll 8
+                    for (int jj = 0; jj < T; ++jj) {
+                        const float4 q = spb[jj];
+#pragma unroll
+                        for (int k = 0; k < IPT; k++) {
+                            const float dx = q.x - px[k], dy = q.y - py[k], dz = q.z - pz[k];
+                            const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                            const float ri = rsqrt_mufu(r2);
+                            const float w = (q.w * ri) * (ri * ri);
+                            fx[k] = fmaf(w, dx, fx[k]);
+                            fy[k] = fmaf(w, dy, fy[k]);
+                            fz[k] = fmaf(w, dz, fz[k]);
+                        }
+                    }
+                } else if (KIND == K_S1_IMG) {
+#pragma unroll 2
+                    for (int jj = 0; jj < T; ++jj) {
+                        const float4 q = spb[jj];
+#pragma unroll
+                        for (int k = 0; k < IPT; k++) {
+                            const float dx = q.x - px[k], dy = q.y - py[k], dz = q.z - pz[k];
+                            const float rho2 = fmaf(dx, dx, dy * dy);
+                            float sw = 0.0f, swz = 0.0f;
+#pragma unroll
+                            for (int m = 0; m < NIMG; m++) {
+                                const float dzm = dz + off[m];
+                                const float ri = rsqrt_mufu(fmaf(dzm, dzm, rho2));
+                                const float ri3 = ri * ri * ri;
+                                sw += ri3;
+                                swz = fmaf(ri3, dzm, swz);
+                            }
+                            const float t = q.w * sw;
+                            fx[k] = fmaf(t, dx, fx[k]);
+                            fy[k] = fmaf(t, dy, fy[k]);
+                            fz[k] = fmaf(q.w, swz, fz[k]);
+                        }
+                    }
+                }
+            } else {
+                // Full path: softening per pair (and per image with the cut test).
+                for (int jj = 0; jj < T; ++jj) {
+                    const float4 q = spb[jj];
+                    const float ej = seb[jj];
+#pragma unroll
+                    for (int k = 0; k < IPT; k++) {
+                        const float dx = q.x - px[k], dy = q.y - py[k];
+                        float dz = q.z - pz[k];
+                        const float b = ei[k] + ej;
+                        const float b2 = b * b;
+                        if (KIND == K_R3) {
+                            const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                            const float ri = rsqrt_mufu(r2);
+                            float w = ri * ri * ri;
+                            if (r2 < b2) w = spline_inner_f32(r2, b);
+                            w *= q.w;
+                            fx[k] = fmaf(w, dx, fx[k]);
+                            fy[k] = fmaf(w, dy, fy[k]);
+                            fz[k] = fmaf(w, dz, fz[k]);
+                        } else {
+                            const float rho2 = fmaf(dx, dx, dy * dy);
+                            int mlo = -a.emax, mhi = a.emax;
+                            if (KIND == K_S1_GEN && a.nearest) {
+                                dz = fabsf(dz) > a.halfL ? dz - copysignf(a.L, dz) : dz;
+                                mlo = mhi = 0;
+                            }
+                            float sw = 0.0f, swz = 0.0f;
+                            for (int m = mlo; m <= mhi; m++) {
+                                const float dzm = dz + (float)m * a.L;
+                                const float r2 = fmaf(dzm, dzm, rho2);
+                                const float ri = rsqrt_mufu(r2);
+                                float w = ri * ri * ri;
+                                if (r2 < b2) w = spline_inner_f32(r2, b);
+                                if (!a.nearest && !(fabsf(dzm) <= a.cutL)) w = 0.0f;
+                                sw += w;
+                                swz = fmaf(w, dzm, swz);
+                            }
+                            const float t = q.w * sw;
+                            fx[k] = fmaf(t, dx, fx[k]);
+                            fy[k] = fmaf(t, dy, fy[k]);
+                            fz[k] = fmaf(q.w, swz, fz[k]);
+                        }
+                    }
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < IPT; k++) {
+                ax[k] += (double)fx[k];
+                ay[k] += (double)fy[k];
+                az[k] += (double)fz[k];
+            }
+            __syncthreads();
+        }
+
+        double *o = a.part + (size_t)chunk * a.part_stride;
+#pragma unroll
+        for (int k = 0; k < IPT; k++) {
+            size_t q = (size_t)I * T + k * BLOCK + tid;
+            o[3 * q] = ax[k];
+            o[3 * q + 1] = ay[k];
+            o[3 * q + 2] = az[k];
+        }
+    }
+}
+
+// Sum the chunk partials in chunk order, add the background term and scatter
+// from curve order back to the caller's order F[3*(orig - id_min) + k].
+__global__ void k_reduce_mixed(const double *__restrict__ part, int S, size_t stride, const uint32_t *__restrict__ perm,
+                               int count, int id_min, const double *__restrict__ x, Background bg,
+                               double *__restrict__ F)
+{
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= count) return;
+    double f[3] = {0, 0, 0};
+    for (int s = 0; s < S; s++)
+        for (int k = 0; k < 3; k++) f[k] += part[(size_t)s * stride + 3 * (size_t)q + k];
+    uint32_t o = perm[q];
+    add_background(bg, x + 3 * (size_t)o, f);
+    for (int k = 0; k < 3; k++) F[3 * (size_t)(o - id_min) + k] = f[k];
+}
+
+using KernelFn = void (*)(MixedArgs);
+
+struct Variant {
+    KernelFn fn;
+    int threads, ipt;
+};
+
+template <int KIND, int EMAX>
+KernelFn pick(int threads, int ipt)
+{
+#define STEPS_SHAPE(B, P) \
+    if (threads == B && ipt == P) return k_pair_mixed<KIND, B, P, EMAX>;
+    STEPS_SHAPE(64, 1) STEPS_SHAPE(64, 2) STEPS_SHAPE(64, 4)
+    STEPS_SHAPE(128, 1) STEPS_SHAPE(128, 2) STEPS_SHAPE(128, 4)
+    STEPS_SHAPE(256, 1) STEPS_SHAPE(256, 2)
+#undef STEPS_SHAPE
+    return nullptr;
+}
+
+KernelFn select_kernel(const KParams &kp, int threads, int ipt)
+{
+    if (kp.topology == STEPS_R3) return pick<K_R3, 0>(threads, ipt);
+    if (kp.topology == STEPS_S1R2 && kp.s1r2_images && kp.is_periodic >= 2) {
+        switch (kp.emax) {
+        case 3: return pick<K_S1_IMG, 3>(threads, ipt);
+        case 4: return pick<K_S1_IMG, 4>(threads, ipt);
+        case 5: return pick<K_S1_IMG, 5>(threads, ipt);
+        default: return pick<K_S1_GEN, 0>(threads, ipt);
+        }
+    }
+    if (kp.topology == STEPS_S1R2 && kp.is_periodic < 2) return pick<K_S1_GEN, 0>(threads, ipt);
+    return nullptr;
+}
+
+}  // namespace
+
+bool shape_supported(int threads, int ipt)
+{
+    KParams kp{};
+    kp.topology = STEPS_R3;
+    return select_kernel(kp, threads, ipt) != nullptr;
+}
+
+bool mixed_supported(const KParams &kp) { return select_kernel(kp, 128, 2) != nullptr; }
+
+void forces_mixed(const KParams &kp, const Tables &tb, const double *x, int n, int id_min, int ni, double *F,
+                  bool reuse_order)
+{
+    Ctx &c = ctx();
+    cudaStream_t st = c.stream;
+    const int threads = c.shape.threads, ipt = c.shape.ipt;
+    const int T = threads * ipt;
+    KernelFn fn = select_kernel(kp, threads, ipt);
+    if (!fn) fail(STEPS_E_ARG, "mixed precision: unsupported topology/mode or kernel shape");
+
+    unsigned long long *bb = c.bbox.ensure<unsigned long long>(8);
+    STEPS_CUDA(cudaEventRecord(c.phase[0], st));
+    build_tiles(c.tj, x, c.m64.as<double>(), c.eps64.as<double>(), 0, n, T, reuse_order, st, bb);
+    const bool full_i = id_min == 0 && ni == n;
+    TileSet &ti = full_i ? c.tj : c.ti;
+    if (!full_i) build_tiles(c.ti, x, c.m64.as<double>(), c.eps64.as<double>(), id_min, ni, T, reuse_order, st, bb);
+    STEPS_CUDA(cudaEventRecord(c.phase[1], st));
+
+    // Work decomposition: items = i tiles x j chunks, sized so the persistent
+    // grid sees several waves with a small last-wave remainder.
+    int occ = 0;
+    STEPS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, threads, 0));
+    if (occ < 1) occ = 1;
+    const int resident = c.nsm * occ;
+    const int nit = ti.ntiles, njt = c.tj.ntiles;
+    int S = c.shape.jsplit;
+    if (S <= 0) {
+        double best = 1e30;
+        S = 1;
+        for (int s = 1; s <= 64 && s <= njt; s++) {
+            int tpc = div_up(njt, s);
+            int sc = div_up(njt, tpc);
+            long long items = (long long)nit * sc;
+            long long waves = (items + resident - 1) / resident;
+            // cost ~ waves * item length, plus a small per-item overhead
+            double cost = (double)waves * tpc + 0.02 * (double)items / resident;
+            if (cost < best - 1e-9) { best = cost; S = s; }
+        }
+    }
+    if (S > njt) S = njt;
+    const int tpc = div_up(njt, S);
+    S = div_up(njt, tpc);
+
+    MixedArgs a;
+    a.jpack = c.tj.pack.as<float4>();
+    a.jeps = c.tj.eps.as<float>();
+    a.jmeta = c.tj.meta.as<float4>();
+    a.njt = njt;
+    a.ipack = ti.pack.as<float4>();
+    a.ieps = ti.eps.as<float>();
+    a.imeta = ti.meta.as<float4>();
+    a.nit = nit;
+    a.S = S;
+    a.tpc = tpc;
+    a.nitems = nit * S;
+    a.counter = c.counter.ensure<unsigned>(4);
+    a.part_stride = (size_t)nit * T * 3;
+    a.part = c.partial.ensure<double>((size_t)S * a.part_stride);
+    a.L = (float)kp.L;
+    a.halfL = (float)kp.halfL;
+    a.cutL = (float)kp.cutL;
+    a.emax = kp.emax;
+    a.nearest = kp.topology == STEPS_S1R2 && kp.is_periodic < 2;
+
+    STEPS_CUDA(cudaMemsetAsync(a.counter, 0, sizeof(unsigned), st));
+    int grid = resident < a.nitems ? resident : a.nitems;
+    fn<<<grid, threads, 0, st>>>(a);
+    note_launch("k_pair_mixed");
+    STEPS_CUDA(cudaEventRecord(c.phase[2], st));
+    k_reduce_mixed<<<div_up(ni, 256), 256, 0, st>>>(a.part, S, a.part_stride, ti.perm(), ni, id_min, x,
+                                                   background_of(kp, tb), F);
+    note_launch("k_reduce_mixed");
+    STEPS_CUDA(cudaEventRecord(c.phase[3], st));
+    c.phase_valid = true;
+    c.last_pairs = (double)ni * (double)n;
+}
+
+}  // namespace steps

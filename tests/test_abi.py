@@ -1,0 +1,50 @@
+"""The C-ABI library builds, loads and exports every entry point that
+include/*.h declares (no GPU needed: nothing is called)."""
+import ctypes
+import glob
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = open(h).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        names |= set(re.findall(r"\b(steps_gpu_\w+)\s*\(", src))
+    return sorted(names)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import steps_gb300 as S
+    if not os.path.exists(S.LIB_PATH):
+        from steps_gb300 import build
+        build.build()
+    return S.load_library()
+
+
+def test_header_declares_entry_points():
+    names = declared_symbols()
+    assert "steps_gpu_forces" in names and "steps_gpu_init" in names
+    assert len(names) >= 20
+
+
+def test_library_exports_every_declared_symbol(lib):
+    missing = [n for n in declared_symbols() if not hasattr(lib, n)]
+    assert not missing, f"not exported: {missing}"
+
+
+def test_calls_without_init_fail_cleanly(lib):
+    # Before steps_gpu_init every entry point reports STEPS_E_STATE (2) and a message.
+    import steps_gb300 as S
+    if lib.steps_gpu_launch_count() != 0:
+        pytest.skip("library already initialised in this process")
+    rc = lib.steps_gpu_set_particles(4, None, None)
+    assert rc == S.STEPS_E_STATE
+    assert b"steps_gpu_init" in lib.steps_gpu_error_string()
+    assert lib.steps_gpu_abi_version() == 1

@@ -1,0 +1,126 @@
+"""S1xR2 and T^3 forces and Ewald tables on the GPU through the C-ABI,
+against the reference's golden vectors and the plain-C oracle."""
+import math
+
+import numpy as np
+import pyoracle as O
+import pytest
+
+import steps_gb300 as S
+from helpers import err_stats, golden, port_params, rel_err
+from steps_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+MIXED_P99 = 1e-5
+
+
+def s1_params(g, isp=2, images=1, order=4, **kw):
+    return S.params(S.S1R2, is_periodic=isp, L=float(g["L"]), rsim=float(g["rsim"]), s1r2_images=images,
+                    ewald_order=order, **kw)
+
+
+def test_s1r2_images_fp64(engine):
+    g = golden("s1r2_images")
+    engine.set_particles(g["m"], g["eps"])
+    assert rel_err(engine.forces(g["x"], s1_params(g, 2), S.FP64), g["F_is2"]).max() < FP64_TOL
+    assert rel_err(engine.forces(g["x"], s1_params(g, 1), S.FP64), g["F_is1"]).max() < FP64_TOL
+    assert rel_err(engine.forces(g["x"], s1_params(g, 4), S.FP64, 0, 255), g["F_is4_head"]).max() < FP64_TOL
+    engine.set_radial_table(g["radial"])
+    p = s1_params(g, 2, cosmology=1, comoving=1, mius=float(g["mius"]))
+    assert rel_err(engine.forces(g["x"], p, S.FP64), g["F_comoving"]).max() < FP64_TOL
+
+
+def test_s1r2_images_mixed(engine):
+    g = golden("s1r2_images")
+    engine.set_particles(g["m"], g["eps"])
+    for isp, key in ((2, "F_is2"), (1, "F_is1")):
+        st = err_stats(engine.forces(g["x"], s1_params(g, isp), S.MIXED), g[key])
+        assert st["p99"] < MIXED_P99, (isp, st)
+    st = err_stats(engine.forces(g["x"], s1_params(g, 4), S.MIXED, 0, 255), g["F_is4_head"])
+    assert st["p99"] < MIXED_P99, st
+    engine.set_radial_table(g["radial"])
+    p = s1_params(g, 2, cosmology=1, comoving=1, mius=float(g["mius"]))
+    assert err_stats(engine.forces(g["x"], p, S.MIXED), g["F_comoving"])["p99"] < MIXED_P99
+
+
+@pytest.mark.parametrize("isp", [3, 15])
+def test_s1r2_other_image_counts(engine, port, isp):
+    ps = W.s1r2_cylindrical(3000, 200.0, 600.0, seed=20 + isp)
+    engine.set_particles(ps.m, ps.eps)
+    s = port.system(3, ps.m, ps.eps, port_params(O, is_periodic=isp, L=200.0, rsim=600.0))
+    Fo = port.forces(s, ps.x, 0, 511)
+    p = S.params(S.S1R2, is_periodic=isp, L=200.0, rsim=600.0, s1r2_images=1)
+    assert rel_err(engine.forces(ps.x, p, S.FP64, 0, 511), Fo).max() < FP64_TOL
+    assert err_stats(engine.forces(ps.x, p, S.MIXED, 0, 511), Fo)["p99"] < MIXED_P99
+
+
+@pytest.mark.parametrize("order", [0, 2, 4])
+def test_s1r2_table_fp64(engine, order):
+    g = golden(f"s1r2_table_o{order}")
+    nrho, nz = (int(v) for v in g["shape"])
+    engine.set_particles(g["m"], g["eps"])
+    engine.set_table_s1r2(g["table"], nrho, nz)
+    F = engine.forces(g["x"], s1_params(g, 2, images=0, order=order), S.FP64)
+    assert rel_err(F, g["F"]).max() < FP64_TOL
+
+
+def test_s1r2_table_builder(engine):
+    g = golden("s1r2_table_o2")
+    nrho, nz = (int(v) for v in g["shape"])
+    alpha, nmax, mmax = g["ewald"]
+    engine.build_table_s1r2(nrho, nz, 2.25 * float(g["rsim"]), float(g["L"]), float(alpha), int(nmax), int(mmax))
+    tab = engine.get_table_s1r2()
+    np.testing.assert_allclose(tab, g["table"], rtol=0, atol=1e-12 * np.abs(g["table"]).max())
+
+
+@pytest.mark.parametrize("order", [2, 4])
+def test_t3_fp64(engine, order):
+    g = golden(f"t3_o{order}")
+    ng, L = int(g["ngrid"]), float(g["L"])
+    engine.set_particles(g["m"], g["eps"])
+    engine.set_table_t3(g["table"], ng)
+    p = S.params(S.T3, is_periodic=2, L=L, rsim=L / 2, ewald_order=order)
+    assert rel_err(engine.forces(g["x"], p, S.FP64), g["F"]).max() < FP64_TOL
+    p = S.params(S.T3, is_periodic=1, L=L, rsim=L / 2, ewald_order=order)
+    assert rel_err(engine.forces(g["x"], p, S.FP64), g["F_nearest"]).max() < FP64_TOL
+
+
+def test_t3_table_builder(engine):
+    g = golden("t3_o4")
+    ng, L = int(g["ngrid"]), float(g["L"])
+    engine.build_table_t3(ng, L, *[float(v) for v in g["ewald"]])
+    tab = engine.get_table_t3()
+    np.testing.assert_allclose(tab, g["table"], rtol=0, atol=1e-13 * np.abs(g["table"]).max())
+    g = golden("t3_table63_sample")
+    engine.build_table_t3(63, 100.0, *[float(v) for v in g["ewald"]])
+    tab = engine.get_table_t3()
+    np.testing.assert_allclose(tab[g["idx"]], g["val"], rtol=0, atol=1e-13 * np.abs(g["val"]).max())
+    # odd symmetry D(-r) = -D(r) of the table (StePS/src/ewald_space.cc:365-376)
+    t = tab.reshape(63, 63, 63, 3)
+    np.testing.assert_array_equal(t[::-1, ::-1, ::-1], -t)
+
+
+def test_t3_lattice_forces_vanish(engine):
+    g = golden("t3_o4")
+    ng, L = int(g["ngrid"]), float(g["L"])
+    k = 5
+    c = (np.arange(k) + 0.5) * L / k
+    x = np.stack(np.meshgrid(c, c, c, indexing="ij"), -1).reshape(-1, 3)
+    n = x.shape[0]
+    engine.set_particles(np.full(n, 1.0), np.full(n, 0.02))
+    engine.set_table_t3(g["table"], ng)
+    F = engine.forces(x, S.params(S.T3, is_periodic=2, L=L, rsim=L / 2, ewald_order=4), S.FP64)
+    assert np.abs(F).max() < 1e-12 * (n / (0.2 * L) ** 2)
+
+
+def test_table_errors(engine):
+    g = golden("t3_o4")
+    engine.set_particles(g["m"], g["eps"])
+    with pytest.raises(S.StepsError) as e:
+        engine.build_table_t3(16, 100.0, 0.02, 2.0, 0.3, 3.0, 6.0)  # even grid
+    assert e.value.code == S.STEPS_E_ARG
+    with pytest.raises(S.StepsError) as e:
+        engine.forces(g["x"], S.params(S.T3, is_periodic=2, L=100.0, ewald_order=3), S.FP64)
+    assert e.value.code == S.STEPS_E_ARG
