@@ -72,6 +72,7 @@ struct TileSet {
     int T = 0, ntiles = 0;
     DevBuf keys[2], vals[2], hist;
     DevBuf pack, eps, meta;
+    DevBuf idx;  // idx[q] = original index of curve position q; padding holds pad_id
     int perm_sel = 0;  // vals[perm_sel] holds curve position -> original index
     bool ordered = false;
     const uint32_t *perm() const { return vals[perm_sel].as<uint32_t>(); }

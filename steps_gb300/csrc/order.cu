@@ -195,7 +195,8 @@ __global__ void __launch_bounds__(TB_THREADS) k_tile_build(const double *__restr
                                                           const double *__restrict__ eps,
                                                           const uint32_t *__restrict__ perm, int count, int T,
                                                           float4 *__restrict__ pack, float *__restrict__ epsf,
-                                                          float4 *__restrict__ meta)
+                                                          float4 *__restrict__ meta, uint32_t *__restrict__ idx,
+                                                          uint32_t pad_id)
 {
     __shared__ double red[7][TB_THREADS / 32];
     __shared__ float s_c[3];
@@ -250,9 +251,11 @@ __global__ void __launch_bounds__(TB_THREADS) k_tile_build(const double *__restr
             pack[q] = make_float4(__double2float_rn(p[0] - cx), __double2float_rn(p[1] - cy),
                                   __double2float_rn(p[2] - cz), __double2float_rn(m[o]));
             epsf[q] = __double2float_rn(eps[o]);
+            if (idx) idx[q] = o;
         } else {
             pack[q] = make_float4(0.f, 0.f, 0.f, 0.f);  // massless padding at the tile centre
             epsf[q] = 0.f;
+            if (idx) idx[q] = pad_id;
         }
     }
 }
@@ -281,7 +284,7 @@ void sort_pairs(TileSet &ts, int n, cudaStream_t st)
 // Orders particles [lo, lo+count) of the AoS FP64 array x along a Morton curve
 // (unless reuse is set and an order already exists) and (re)builds the tiles.
 void build_tiles(TileSet &ts, const double *x, const double *m64, const double *eps64, int lo, int count, int T,
-                 bool reuse, cudaStream_t st, unsigned long long *bbox_scratch)
+                 bool reuse, cudaStream_t st, unsigned long long *bbox_scratch, uint32_t pad_id)
 {
     if (count <= 0) fail(STEPS_E_ARG, "empty particle set");
     bool same = ts.ordered && ts.lo == lo && ts.count == count;
@@ -309,8 +312,10 @@ void build_tiles(TileSet &ts, const double *x, const double *m64, const double *
     ts.pack.ensure<float4>(padded);
     ts.eps.ensure<float>(padded);
     ts.meta.ensure<float4>(2 * (size_t)ts.ntiles);
+    ts.idx.ensure<uint32_t>(padded);
     k_tile_build<<<ts.ntiles, TB_THREADS, 0, st>>>(x, m64, eps64, ts.perm(), count, T, ts.pack.as<float4>(),
-                                                   ts.eps.as<float>(), ts.meta.as<float4>());
+                                                   ts.eps.as<float>(), ts.meta.as<float4>(), ts.idx.as<uint32_t>(),
+                                                   pad_id);
     note_launch("k_tile_build");
 }
 
@@ -329,10 +334,10 @@ void batch_keys(const double *x, int lo, int count, unsigned long long prefix, u
 }
 
 void tile_build_range(const double *x, const double *m64, const double *eps64, const uint32_t *perm, int count, int T,
-                      float4 *pack, float *epsf, float4 *meta, cudaStream_t st)
+                      float4 *pack, float *epsf, float4 *meta, uint32_t *idx, uint32_t pad_id, cudaStream_t st)
 {
     int nt = div_up(count, T);
-    k_tile_build<<<nt, TB_THREADS, 0, st>>>(x, m64, eps64, perm, count, T, pack, epsf, meta);
+    k_tile_build<<<nt, TB_THREADS, 0, st>>>(x, m64, eps64, perm, count, T, pack, epsf, meta, idx, pad_id);
     note_launch("k_tile_build");
 }
 

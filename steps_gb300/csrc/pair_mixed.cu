@@ -35,10 +35,12 @@ struct MixedArgs {
     const float4 *jpack;
     const float *jeps;
     const float4 *jmeta;
+    const uint32_t *jidx;
     int njt;
     const float4 *ipack;
     const float *ieps;
     const float4 *imeta;
+    const uint32_t *iidx;
     int nit;
     int S, tpc;  // j chunks per i tile, j tiles per chunk
     int nitems;
@@ -65,7 +67,7 @@ template <int N>
 __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
 
 template <int BLOCK, int IPT>
-__device__ __forceinline__ void stage_tile(const MixedArgs &a, int J, float4 *sp, float *se)
+__device__ __forceinline__ void stage_tile(const MixedArgs &a, int J, float4 *sp, float *se, uint32_t *sid)
 {
     constexpr int T = BLOCK * IPT;
 #pragma unroll
@@ -74,6 +76,7 @@ __device__ __forceinline__ void stage_tile(const MixedArgs &a, int J, float4 *sp
         size_t q = (size_t)J * T + e;
         cp_async16(sp + e, a.jpack + q);
         cp_async4(se + e, a.jeps + q);
+        cp_async4(sid + e, a.jidx + q);
     }
     cp_commit();
 }
@@ -88,6 +91,7 @@ __global__ void __launch_bounds__(BLOCK) k_pair_mixed(MixedArgs a)
     constexpr int NIMG = KIND == K_S1_IMG ? 2 * EMAX + 1 : 1;
     __shared__ __align__(16) float4 sp[2][T];
     __shared__ __align__(16) float se[2][T];
+    __shared__ __align__(16) uint32_t sid[2][T];
     __shared__ int s_item;
     const int tid = threadIdx.x;
 
@@ -105,6 +109,7 @@ __global__ void __launch_bounds__(BLOCK) k_pair_mixed(MixedArgs a)
         const float4 mI0 = __ldg(a.imeta + 2 * I);
         const float4 mI1 = __ldg(a.imeta + 2 * I + 1);
         float xi[IPT], yi[IPT], zi[IPT], ei[IPT];
+        uint32_t ii[IPT];
         double ax[IPT], ay[IPT], az[IPT];
 #pragma unroll
         for (int k = 0; k < IPT; k++) {
@@ -114,14 +119,15 @@ __global__ void __launch_bounds__(BLOCK) k_pair_mixed(MixedArgs a)
             yi[k] = p.y;
             zi[k] = p.z;
             ei[k] = __ldg(a.ieps + q);
+            ii[k] = __ldg(a.iidx + q);
             ax[k] = ay[k] = az[k] = 0.0;
         }
 
-        if (J0 < J1) stage_tile<BLOCK, IPT>(a, J0, sp[0], se[0]);
+        if (J0 < J1) stage_tile<BLOCK, IPT>(a, J0, sp[0], se[0], sid[0]);
         for (int J = J0; J < J1; ++J) {
             const int buf = (J - J0) & 1;
             if (J + 1 < J1) {
-                stage_tile<BLOCK, IPT>(a, J + 1, sp[buf ^ 1], se[buf ^ 1]);
+                stage_tile<BLOCK, IPT>(a, J + 1, sp[buf ^ 1], se[buf ^ 1], sid[buf ^ 1]);
                 cp_wait<1>();
             } else {
                 cp_wait<0>();
@@ -175,6 +181,7 @@ __global__ void __launch_bounds__(BLOCK) k_pair_mixed(MixedArgs a)
             }
             const float4 *spb = sp[buf];
             const float *seb = se[buf];
+            const uint32_t *sidb = sid[buf];
 
             if (!full) {
                 if (KIND == K_R3) {
@@ -218,13 +225,18 @@ __global__ void __launch_bounds__(BLOCK) k_pair_mixed(MixedArgs a)
                 }
             } else {
                 // Full path: softening per pair (and per image with the cut test).
+                // The self pair gets d = 0 exactly, as in the reference: after
+                // the change of tile frame its FP32 separation is a rounding
+                // residue, which the spline core would turn into a force.
                 for (int jj = 0; jj < T; ++jj) {
                     const float4 q = spb[jj];
                     const float ej = seb[jj];
+                    const uint32_t jid = sidb[jj];
 #pragma unroll
                     for (int k = 0; k < IPT; k++) {
-                        const float dx = q.x - px[k], dy = q.y - py[k];
-                        float dz = q.z - pz[k];
+                        const bool self = jid == ii[k];
+                        const float dx = self ? 0.0f : q.x - px[k], dy = self ? 0.0f : q.y - py[k];
+                        float dz = self ? 0.0f : q.z - pz[k];
                         const float b = ei[k] + ej;
                         const float b2 = b * b;
                         if (KIND == K_R3) {
@@ -355,10 +367,11 @@ void forces_mixed(const KParams &kp, const Tables &tb, const double *x, int n, i
 
     unsigned long long *bb = c.bbox.ensure<unsigned long long>(8);
     STEPS_CUDA(cudaEventRecord(c.phase[0], st));
-    build_tiles(c.tj, x, c.m64.as<double>(), c.eps64.as<double>(), 0, n, T, reuse_order, st, bb);
+    build_tiles(c.tj, x, c.m64.as<double>(), c.eps64.as<double>(), 0, n, T, reuse_order, st, bb, PAD_J);
     const bool full_i = id_min == 0 && ni == n;
     TileSet &ti = full_i ? c.tj : c.ti;
-    if (!full_i) build_tiles(c.ti, x, c.m64.as<double>(), c.eps64.as<double>(), id_min, ni, T, reuse_order, st, bb);
+    if (!full_i)
+        build_tiles(c.ti, x, c.m64.as<double>(), c.eps64.as<double>(), id_min, ni, T, reuse_order, st, bb, PAD_I);
     STEPS_CUDA(cudaEventRecord(c.phase[1], st));
 
     // Work decomposition: items = i tiles x j chunks, sized so the persistent
@@ -390,10 +403,12 @@ void forces_mixed(const KParams &kp, const Tables &tb, const double *x, int n, i
     a.jpack = c.tj.pack.as<float4>();
     a.jeps = c.tj.eps.as<float>();
     a.jmeta = c.tj.meta.as<float4>();
+    a.jidx = c.tj.idx.as<uint32_t>();
     a.njt = njt;
     a.ipack = ti.pack.as<float4>();
     a.ieps = ti.eps.as<float>();
     a.imeta = ti.meta.as<float4>();
+    a.iidx = ti.idx.as<uint32_t>();
     a.nit = nit;
     a.S = S;
     a.tpc = tpc;
