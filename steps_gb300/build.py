@@ -34,12 +34,19 @@ def _flags():
                    "-I", CSRC, "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 
 
+# The Ewald table builders decide which lattice terms enter by comparing
+# squared distances with the cut exactly as the reference does (separately
+# rounded products, no FMA contraction); contracting changes those decisions
+# and the cell-centre coordinates (the reference's centre cell is exactly 0).
+PER_FILE_FLAGS = {"ewald.cu": ["-fmad=false"]}
+
+
 def _compile(src: str, verbose: bool) -> str:
     obj = os.path.join(OUT_DIR, os.path.basename(src) + ".o")
-    deps = [src] + glob.glob(os.path.join(CSRC, "*.cuh")) + [os.path.join(ROOT, "include", "steps_gb300.h")]
+    deps = [src, __file__] + glob.glob(os.path.join(CSRC, "*.cuh")) + [os.path.join(ROOT, "include", "steps_gb300.h")]
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps):
         return obj
-    cmd = [nvcc_path()] + _flags() + ["-c", src, "-o", obj]
+    cmd = [nvcc_path()] + _flags() + PER_FILE_FLAGS.get(os.path.basename(src), []) + ["-c", src, "-o", obj]
     if verbose:
         print(" ".join(cmd), flush=True)
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -220,7 +220,7 @@ int steps_gpu_shutdown(void)
         TileSet *ts[] = {&c.tj, &c.ti};
         for (TileSet *t : ts) {
             for (int k = 0; k < 2; k++) { t->keys[k].release(); t->vals[k].release(); }
-            t->hist.release(); t->pack.release(); t->eps.release(); t->meta.release(); t->idx.release();
+            t->hist.release(); t->pack.release(); t->eps.release(); t->meta.release(); t->idx.release(); t->resid.release();
             *t = TileSet();
         }
         for (auto &e : c.marks) cudaEventDestroy(e);

@@ -73,6 +73,7 @@ struct TileSet {
     DevBuf keys[2], vals[2], hist;
     DevBuf pack, eps, meta;
     DevBuf idx;  // idx[q] = original index of curve position q; padding holds pad_id
+    DevBuf resid;  // resid[q] = (x - c) - pack[q].xyz, the FP32 residual of the offset
     int perm_sel = 0;  // vals[perm_sel] holds curve position -> original index
     bool ordered = false;
     const uint32_t *perm() const { return vals[perm_sel].as<uint32_t>(); }

@@ -60,7 +60,8 @@ void sort_pairs(TileSet &ts, int n, cudaStream_t st);
 void batch_keys(const double *x, int lo, int count, unsigned long long prefix, unsigned long long *keys, uint32_t *vals,
                 unsigned long long *bbox_scratch, cudaStream_t st);
 void tile_build_range(const double *x, const double *m64, const double *eps64, const uint32_t *perm, int count, int T,
-                      float4 *pack, float *epsf, float4 *meta, uint32_t *idx, uint32_t pad_id, cudaStream_t st);
+                      float4 *pack, float *epsf, float4 *meta, uint32_t *idx, uint32_t pad_id, float4 *lo,
+                      cudaStream_t st);
 
 // pair_fp64.cu: FP64 forces of i in [id_min, id_min+ni) into F[3*ni] (with background).
 void forces_fp64(const KParams &kp, const Tables &tb, const double *x, int n, int id_min, int ni, double *F);

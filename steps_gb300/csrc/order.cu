@@ -196,7 +196,7 @@ __global__ void __launch_bounds__(TB_THREADS) k_tile_build(const double *__restr
                                                           const uint32_t *__restrict__ perm, int count, int T,
                                                           float4 *__restrict__ pack, float *__restrict__ epsf,
                                                           float4 *__restrict__ meta, uint32_t *__restrict__ idx,
-                                                          uint32_t pad_id)
+                                                          uint32_t pad_id, float4 *__restrict__ lo)
 {
     __shared__ double red[7][TB_THREADS / 32];
     __shared__ float s_c[3];
@@ -248,12 +248,19 @@ __global__ void __launch_bounds__(TB_THREADS) k_tile_build(const double *__restr
         if (q < count) {
             uint32_t o = perm[q];
             const double *p = x + 3 * (size_t)o;
-            pack[q] = make_float4(__double2float_rn(p[0] - cx), __double2float_rn(p[1] - cy),
-                                  __double2float_rn(p[2] - cz), __double2float_rn(m[o]));
+            const double ox = p[0] - cx, oy = p[1] - cy, oz = p[2] - cz;
+            const float hx = __double2float_rn(ox), hy = __double2float_rn(oy), hz = __double2float_rn(oz);
+            pack[q] = make_float4(hx, hy, hz, __double2float_rn(m[o]));
+            // What FP32 dropped from the offset: i particles carry it so that
+            // their position in another tile's frame keeps full precision.
+            if (lo)
+                lo[q] = make_float4(__double2float_rn(ox - hx), __double2float_rn(oy - hy), __double2float_rn(oz - hz),
+                                    0.f);
             epsf[q] = __double2float_rn(eps[o]);
             if (idx) idx[q] = o;
         } else {
             pack[q] = make_float4(0.f, 0.f, 0.f, 0.f);  // massless padding at the tile centre
+            if (lo) lo[q] = make_float4(0.f, 0.f, 0.f, 0.f);
             epsf[q] = 0.f;
             if (idx) idx[q] = pad_id;
         }
@@ -313,9 +320,10 @@ void build_tiles(TileSet &ts, const double *x, const double *m64, const double *
     ts.eps.ensure<float>(padded);
     ts.meta.ensure<float4>(2 * (size_t)ts.ntiles);
     ts.idx.ensure<uint32_t>(padded);
+    ts.resid.ensure<float4>(padded);
     k_tile_build<<<ts.ntiles, TB_THREADS, 0, st>>>(x, m64, eps64, ts.perm(), count, T, ts.pack.as<float4>(),
                                                    ts.eps.as<float>(), ts.meta.as<float4>(), ts.idx.as<uint32_t>(),
-                                                   pad_id);
+                                                   pad_id, ts.resid.as<float4>());
     note_launch("k_tile_build");
 }
 
@@ -334,10 +342,11 @@ void batch_keys(const double *x, int lo, int count, unsigned long long prefix, u
 }
 
 void tile_build_range(const double *x, const double *m64, const double *eps64, const uint32_t *perm, int count, int T,
-                      float4 *pack, float *epsf, float4 *meta, uint32_t *idx, uint32_t pad_id, cudaStream_t st)
+                      float4 *pack, float *epsf, float4 *meta, uint32_t *idx, uint32_t pad_id, float4 *lo,
+                      cudaStream_t st)
 {
     int nt = div_up(count, T);
-    k_tile_build<<<nt, TB_THREADS, 0, st>>>(x, m64, eps64, perm, count, T, pack, epsf, meta, idx, pad_id);
+    k_tile_build<<<nt, TB_THREADS, 0, st>>>(x, m64, eps64, perm, count, T, pack, epsf, meta, idx, pad_id, lo);
     note_launch("k_tile_build");
 }
 

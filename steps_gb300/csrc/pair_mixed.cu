@@ -41,6 +41,7 @@ struct MixedArgs {
     const float *ieps;
     const float4 *imeta;
     const uint32_t *iidx;
+    const float4 *ilo;
     int nit;
     int S, tpc;  // j chunks per i tile, j tiles per chunk
     int nitems;
@@ -81,6 +82,15 @@ __device__ __forceinline__ void stage_tile(const MixedArgs &a, int J, float4 *sp
     cp_commit();
 }
 
+// a - b = s + e exactly (Knuth's TwoSum on a + (-b)); returns s, writes e.
+__device__ __forceinline__ float two_diff(float a, float b, float &e)
+{
+    const float s = a - b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (-b - bb);
+    return s;
+}
+
 // Lower bound of |d| over the separations of two boxes along one axis.
 __device__ __forceinline__ float axis_gap(float dO, float hI, float hJ) { return fmaxf(fabsf(dO) - hI - hJ, 0.0f); }
 
@@ -108,7 +118,7 @@ __global__ void __launch_bounds__(BLOCK) k_pair_mixed(MixedArgs a)
 
         const float4 mI0 = __ldg(a.imeta + 2 * I);
         const float4 mI1 = __ldg(a.imeta + 2 * I + 1);
-        float xi[IPT], yi[IPT], zi[IPT], ei[IPT];
+        float xi[IPT], yi[IPT], zi[IPT], ei[IPT], lx[IPT], ly[IPT], lz[IPT];
         uint32_t ii[IPT];
         double ax[IPT], ay[IPT], az[IPT];
 #pragma unroll
@@ -120,6 +130,10 @@ __global__ void __launch_bounds__(BLOCK) k_pair_mixed(MixedArgs a)
             zi[k] = p.z;
             ei[k] = __ldg(a.ieps + q);
             ii[k] = __ldg(a.iidx + q);
+            const float4 l = __ldg(a.ilo + q);
+            lx[k] = l.x;
+            ly[k] = l.y;
+            lz[k] = l.z;
             ax[k] = ay[k] = az[k] = 0.0;
         }
 
@@ -136,7 +150,12 @@ __global__ void __launch_bounds__(BLOCK) k_pair_mixed(MixedArgs a)
 
             const float4 mJ0 = __ldg(a.jmeta + 2 * J);
             const float4 mJ1 = __ldg(a.jmeta + 2 * J + 1);
-            const float dOx = mJ0.x - mI0.x, dOy = mJ0.y - mI0.y, dOz = mJ0.z - mI0.z;
+            // d_O = c_J - c_I as an unevaluated FP32 sum dO + eO (TwoSum,
+            // exact): the i particles' positions in J's frame then carry
+            // ~1e-7 of |x_i - c_J| whatever the size of the i tile.
+            float eOx, eOy, eOz;
+            const float dOx = two_diff(mJ0.x, mI0.x, eOx), dOy = two_diff(mJ0.y, mI0.y, eOy),
+                        dOz = two_diff(mJ0.z, mI0.z, eOz);
             const float bmax = mI0.w + mJ0.w;
             const float bmax2 = bmax * bmax * 1.0001f + 1e-30f;
             const float gx = axis_gap(dOx, mI1.x, mJ1.x), gy = axis_gap(dOy, mI1.y, mJ1.y);
@@ -174,9 +193,9 @@ __global__ void __launch_bounds__(BLOCK) k_pair_mixed(MixedArgs a)
             float px[IPT], py[IPT], pz[IPT], fx[IPT], fy[IPT], fz[IPT];
 #pragma unroll
             for (int k = 0; k < IPT; k++) {
-                px[k] = xi[k] - dOx;
-                py[k] = yi[k] - dOy;
-                pz[k] = zi[k] - dOz;
+                px[k] = ((xi[k] - dOx) - eOx) + lx[k];
+                py[k] = ((yi[k] - dOy) - eOy) + ly[k];
+                pz[k] = ((zi[k] - dOz) - eOz) + lz[k];
                 fx[k] = fy[k] = fz[k] = 0.0f;
             }
             const float4 *spb = sp[buf];
@@ -409,6 +428,7 @@ void forces_mixed(const KParams &kp, const Tables &tb, const double *x, int n, i
     a.ieps = ti.eps.as<float>();
     a.imeta = ti.meta.as<float4>();
     a.iidx = ti.idx.as<uint32_t>();
+    a.ilo = ti.resid.as<float4>();
     a.nit = nit;
     a.S = S;
     a.tpc = tpc;
