@@ -215,7 +215,7 @@ int steps_gpu_shutdown(void)
         cudaStreamSynchronize(c.stream);
         batch_release();
         DevBuf *bufs[] = {&c.m64, &c.eps64, &c.x, &c.v, &c.F, &c.pack64, &c.partial, &c.bbox, &c.counter,
-                          &c.status, &c.flush, &c.peaks, &c.t3, &c.s1r2, &c.radial};
+                          &c.status, &c.flush, &c.peaks, &c.t3, &c.t3f, &c.s1r2, &c.radial};
         for (DevBuf *b : bufs) b->release();
         TileSet *ts[] = {&c.tj, &c.ti};
         for (TileSet *t : ts) {
@@ -344,6 +344,7 @@ int steps_gpu_set_table_t3(int ngrid, const double *table)
                                    c.stream));
         STEPS_CUDA(cudaStreamSynchronize(c.stream));
         c.t3_ng = ngrid;
+        c.t3_version++;
     });
 }
 
@@ -419,11 +420,13 @@ int steps_gpu_autotune(const steps_params *p, int id_min, int id_max, int *out)
     return guarded([&] {
         require_init();
         Ctx &c = g_ctx;
-        static const int shapes[][2] = {{64, 2}, {64, 4}, {128, 1}, {128, 2}, {128, 4}, {256, 1}, {256, 2}};
+        static const int shapes[][2] = {{64, 1}, {64, 2}, {64, 4}, {128, 1}, {128, 2}, {128, 4}, {256, 1}, {256, 2}};
         Shape keep = c.shape;
         float best = 1e30f;
         Shape bestS = keep;
+        KParams kp = derive_params(p);
         for (auto &s : shapes) {
+            if (!shape_supported_for(kp, s[0], s[1])) continue;
             c.shape.threads = s[0];
             c.shape.ipt = s[1];
             c.shape.jsplit = 0;

@@ -31,6 +31,9 @@ struct Ctx {
 
     DevBuf t3;
     int t3_ng = 0;
+    long long t3_version = 0;  // bumped whenever the table changes
+    DevBuf t3f;                // FP32 float4-per-cell copy for the mixed kernels
+    long long t3f_version = -1;
     DevBuf s1r2;
     int nrho = 0, nz = 0;
     DevBuf radial;
@@ -71,6 +74,7 @@ struct MixedLaunch;
 void forces_mixed(const KParams &kp, const Tables &tb, const double *x, int n, int id_min, int ni, double *F,
                   bool reuse_order);
 bool shape_supported(int threads, int ipt);
+bool shape_supported_for(const KParams &kp, int threads, int ipt);
 
 // Shared force driver used by the C-ABI, the KDK loop and the batch code.
 void compute_forces(const steps_params *p, int precision, int id_min, int id_max, bool reuse_order);

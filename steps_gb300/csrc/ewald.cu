@@ -287,6 +287,7 @@ int steps_gpu_build_table_t3(int ngrid, double L, double alpha, double rel_cut, 
             dri.release();
             dki.release();
             c.t3_ng = a.ngrid;
+            c.t3_version++;
         },
         &a);
 }

@@ -1,0 +1,89 @@
+// Shared pieces of the mixed-precision pair kernels (pair_mixed.cu, pair_t3.cu):
+// the argument block, cp.async staging of j tiles, TwoSum and box gaps.
+#pragma once
+
+#include "common.cuh"
+
+namespace steps {
+namespace mixed {
+
+enum Kind { K_R3 = 0, K_S1_IMG = 1, K_S1_GEN = 2 };
+
+struct MixedArgs {
+    const float4 *jpack;
+    const float *jeps;
+    const float4 *jmeta;
+    const uint32_t *jidx;
+    int njt;
+    const float4 *ipack;
+    const float *ieps;
+    const float4 *imeta;
+    const uint32_t *iidx;
+    const float4 *ilo;
+    int nit;
+    int S, tpc;  // j chunks per i tile, j tiles per chunk
+    int nitems;
+    unsigned *counter;
+    double *part;       // [S][nit*T][3]
+    size_t part_stride; // nit*T*3
+    float L, halfL, cutL;
+    int emax;
+    int nearest;        // S1R2 IS_PERIODIC == 1: nearest image along z only
+    // T^3 Ewald table (FP32 copy, one float4 per cell) and its geometry
+    const float4 *t3f;
+    int ng;
+    float ih, u0;       // continuous cell index u(d) = d * ih + u0, ih = ng / L, u0 = ng/2 - 1/2
+    int wcap;           // cells of the shared-memory table window
+};
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+{
+    unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem)
+{
+    unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem));
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+template <int BLOCK, int IPT>
+__device__ __forceinline__ void stage_tile(const MixedArgs &a, int J, float4 *sp, float *se, uint32_t *sid)
+{
+    constexpr int T = BLOCK * IPT;
+#pragma unroll
+    for (int k = 0; k < IPT; k++) {
+        int e = k * BLOCK + threadIdx.x;
+        size_t q = (size_t)J * T + e;
+        cp_async16(sp + e, a.jpack + q);
+        cp_async4(se + e, a.jeps + q);
+        cp_async4(sid + e, a.jidx + q);
+    }
+    cp_commit();
+}
+
+// a - b = s + e exactly (Knuth's TwoSum on a + (-b)); returns s, writes e.
+__device__ __forceinline__ float two_diff(float a, float b, float &e)
+{
+    const float s = a - b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (-b - bb);
+    return s;
+}
+
+// Lower bound of |d| over the separations of two boxes along one axis.
+__device__ __forceinline__ float axis_gap(float dO, float hI, float hJ) { return fmaxf(fabsf(dO) - hI - hJ, 0.0f); }
+
+using KernelFn = void (*)(MixedArgs);
+
+}  // namespace mixed
+
+// pair_t3.cu: T^3 kernel for a shape (dynamic shared memory returned) and its
+// table arguments (FP32 table copy, grid geometry).
+mixed::KernelFn t3_kernel(const KParams &kp, int threads, int ipt, size_t *dyn_smem);
+void t3_args(mixed::MixedArgs &a, const KParams &kp, const Tables &tb, cudaStream_t st);
+
+}  // namespace steps

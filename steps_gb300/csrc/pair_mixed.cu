@@ -24,75 +24,13 @@
 // 3 FFMA per pair); near ones run the full spline (forces.cc:52-87).
 #include "common.cuh"
 #include "context.cuh"
+#include "mixed.cuh"
 
 namespace steps {
 
 namespace {
 
-enum Kind { K_R3 = 0, K_S1_IMG = 1, K_S1_GEN = 2 };
-
-struct MixedArgs {
-    const float4 *jpack;
-    const float *jeps;
-    const float4 *jmeta;
-    const uint32_t *jidx;
-    int njt;
-    const float4 *ipack;
-    const float *ieps;
-    const float4 *imeta;
-    const uint32_t *iidx;
-    const float4 *ilo;
-    int nit;
-    int S, tpc;  // j chunks per i tile, j tiles per chunk
-    int nitems;
-    unsigned *counter;
-    double *part;       // [S][nit*T][3]
-    size_t part_stride; // nit*T*3
-    float L, halfL, cutL;
-    int emax;
-    int nearest;        // S1R2 IS_PERIODIC == 1: nearest image along z only
-};
-
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
-{
-    unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
-}
-__device__ __forceinline__ void cp_async4(void *smem, const void *gmem)
-{
-    unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem));
-}
-__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::); }
-template <int N>
-__device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
-
-template <int BLOCK, int IPT>
-__device__ __forceinline__ void stage_tile(const MixedArgs &a, int J, float4 *sp, float *se, uint32_t *sid)
-{
-    constexpr int T = BLOCK * IPT;
-#pragma unroll
-    for (int k = 0; k < IPT; k++) {
-        int e = k * BLOCK + threadIdx.x;
-        size_t q = (size_t)J * T + e;
-        cp_async16(sp + e, a.jpack + q);
-        cp_async4(se + e, a.jeps + q);
-        cp_async4(sid + e, a.jidx + q);
-    }
-    cp_commit();
-}
-
-// a - b = s + e exactly (Knuth's TwoSum on a + (-b)); returns s, writes e.
-__device__ __forceinline__ float two_diff(float a, float b, float &e)
-{
-    const float s = a - b;
-    const float bb = s - a;
-    e = (a - (s - bb)) + (-b - bb);
-    return s;
-}
-
-// Lower bound of |d| over the separations of two boxes along one axis.
-__device__ __forceinline__ float axis_gap(float dO, float hI, float hJ) { return fmaxf(fabsf(dO) - hI - hJ, 0.0f); }
+using namespace mixed;
 
 template <int KIND, int BLOCK, int IPT, int EMAX>
 __global__ void __launch_bounds__(BLOCK) k_pair_mixed(MixedArgs a)
@@ -329,13 +267,6 @@ __global__ void k_reduce_mixed(const double *__restrict__ part, int S, size_t st
     for (int k = 0; k < 3; k++) F[3 * (size_t)(o - id_min) + k] = f[k];
 }
 
-using KernelFn = void (*)(MixedArgs);
-
-struct Variant {
-    KernelFn fn;
-    int threads, ipt;
-};
-
 template <int KIND, int EMAX>
 KernelFn pick(int threads, int ipt)
 {
@@ -372,6 +303,13 @@ bool shape_supported(int threads, int ipt)
     return select_kernel(kp, threads, ipt) != nullptr;
 }
 
+bool shape_supported_for(const KParams &kp, int threads, int ipt)
+{
+    size_t dyn;
+    if (kp.topology == STEPS_T3) return t3_kernel(kp, threads, ipt, &dyn) != nullptr;
+    return select_kernel(kp, threads, ipt) != nullptr;
+}
+
 bool mixed_supported(const KParams &kp) { return select_kernel(kp, 128, 2) != nullptr; }
 
 void forces_mixed(const KParams &kp, const Tables &tb, const double *x, int n, int id_min, int ni, double *F,
@@ -381,7 +319,8 @@ void forces_mixed(const KParams &kp, const Tables &tb, const double *x, int n, i
     cudaStream_t st = c.stream;
     const int threads = c.shape.threads, ipt = c.shape.ipt;
     const int T = threads * ipt;
-    KernelFn fn = select_kernel(kp, threads, ipt);
+    size_t dyn = 0;
+    KernelFn fn = kp.topology == STEPS_T3 ? t3_kernel(kp, threads, ipt, &dyn) : select_kernel(kp, threads, ipt);
     if (!fn) fail(STEPS_E_ARG, "mixed precision: unsupported topology/mode or kernel shape");
 
     unsigned long long *bb = c.bbox.ensure<unsigned long long>(8);
@@ -396,7 +335,7 @@ void forces_mixed(const KParams &kp, const Tables &tb, const double *x, int n, i
     // Work decomposition: items = i tiles x j chunks, sized so the persistent
     // grid sees several waves with a small last-wave remainder.
     int occ = 0;
-    STEPS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, threads, 0));
+    STEPS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, threads, dyn));
     if (occ < 1) occ = 1;
     const int resident = c.nsm * occ;
     const int nit = ti.ntiles, njt = c.tj.ntiles;
@@ -441,10 +380,15 @@ void forces_mixed(const KParams &kp, const Tables &tb, const double *x, int n, i
     a.cutL = (float)kp.cutL;
     a.emax = kp.emax;
     a.nearest = kp.topology == STEPS_S1R2 && kp.is_periodic < 2;
+    a.t3f = nullptr;
+    a.ng = 0;
+    a.ih = a.u0 = 0.0f;
+    a.wcap = 0;
+    if (kp.topology == STEPS_T3) t3_args(a, kp, tb, st);
 
     STEPS_CUDA(cudaMemsetAsync(a.counter, 0, sizeof(unsigned), st));
     int grid = resident < a.nitems ? resident : a.nitems;
-    fn<<<grid, threads, 0, st>>>(a);
+    fn<<<grid, threads, dyn, st>>>(a);
     note_launch("k_pair_mixed");
     STEPS_CUDA(cudaEventRecord(c.phase[2], st));
     k_reduce_mixed<<<div_up(ni, 256), 256, 0, st>>>(a.part, S, a.part_stride, ti.perm(), ni, id_min, x,

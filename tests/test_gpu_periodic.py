@@ -124,3 +124,42 @@ def test_table_errors(engine):
     with pytest.raises(S.StepsError) as e:
         engine.forces(g["x"], S.params(S.T3, is_periodic=2, L=100.0, ewald_order=3), S.FP64)
     assert e.value.code == S.STEPS_E_ARG
+
+
+@pytest.mark.parametrize("order", [2, 4])
+def test_t3_mixed(engine, order):
+    g = golden(f"t3_o{order}")
+    ng, L = int(g["ngrid"]), float(g["L"])
+    engine.set_particles(g["m"], g["eps"])
+    engine.set_table_t3(g["table"], ng)
+    p = S.params(S.T3, is_periodic=2, L=L, rsim=L / 2, ewald_order=order)
+    st = err_stats(engine.forces(g["x"], p, S.MIXED), g["F"])
+    assert st["p99"] < MIXED_P99, st
+    st = err_stats(engine.forces(g["x"], p, S.MIXED, 300, 1000), g["F"][300:1001])
+    assert st["p99"] < MIXED_P99, st
+    p = S.params(S.T3, is_periodic=1, L=L, rsim=L / 2, ewald_order=order)
+    st = err_stats(engine.forces(g["x"], p, S.MIXED), g["F_nearest"])
+    assert st["p99"] < MIXED_P99, st
+
+
+@pytest.mark.parametrize("order", [2, 4])
+def test_t3_mixed_shapes_and_workload_table(engine, port, order):
+    """The T^3 workload's own table (Ng = 63, built on the GPU) on a clumpy
+    set: every kernel shape against the FP64 kernel, with the window fallback
+    exercised by the larger tiles."""
+    g = golden("t3_table63_sample")
+    ps = W.t3_clumpy(6000, 100.0, seed=31, n_clumps=24)
+    engine.set_particles(ps.m, ps.eps)
+    engine.build_table_t3(63, 100.0, *[float(v) for v in g["ewald"]])
+    p = S.params(S.T3, is_periodic=2, L=100.0, rsim=50.0, ewald_order=order)
+    F64 = engine.forces(ps.x, p, S.FP64)
+    tab = engine.get_table_t3(63)
+    s = port.system(1, ps.m, ps.eps, port_params(O, is_periodic=2, L=100.0, rsim=50.0), table=tab, ngrid=63,
+                    order=order)
+    Fo = port.forces(s, ps.x, 0, 255)
+    assert rel_err(F64[:256], Fo).max() < FP64_TOL
+    for threads, ipt in ((64, 1), (64, 2), (128, 1), (128, 2), (256, 1)):
+        engine.set_tuning(threads, ipt, 0)
+        st = err_stats(engine.forces(ps.x, p, S.MIXED), F64)
+        assert st["p99"] < MIXED_P99, (threads, ipt, st)
+    engine.set_tuning(128, 2, 0)
