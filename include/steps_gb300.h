@@ -186,8 +186,14 @@ int steps_gpu_batch_get(int k, double *x, double *v, double *F);
  * is threads*ipt. Returns STEPS_E_ARG for an unsupported shape. */
 int steps_gpu_set_tuning(int threads, int ipt, int jsplit);
 
-/* Times every supported mixed-precision shape on the resident particles for
- * the given topology and keeps the fastest; writes threads, ipt to out[2]. */
+/* R^3 mixed-precision pair loop: 0 = scalar FP32 instructions, 1 = packed
+ * FP32x2 instructions (two pairs per instruction, sm_100+). Same results to
+ * rounding; the autotuner picks between them. */
+int steps_gpu_set_kernel_variant(int variant);
+
+/* Times every supported mixed-precision shape (and, for R^3, both pair-loop
+ * variants) on the resident particles for the given topology and keeps the
+ * fastest; writes threads, ipt, variant to out[3]. */
 int steps_gpu_autotune(const steps_params *p, int id_min, int id_max, int *out);
 
 /* Number of kernels this library has launched since init. */

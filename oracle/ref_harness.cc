@@ -214,7 +214,11 @@ void ref_get_state(double *xo, double *vo, double *Fo)
     for (int i = 0; i < 3 * N; i++) { xo[i] = x[i]; vo[i] = v[i]; Fo[i] = F[i]; }
 }
 
+#ifndef STEPS_HARNESS_NO_SOFTENING_PROBE
+/* force_softening lives in the reference's force TU (forces.cc:52); a build
+ * that links another force TU (tests/test_legacy_link.py) leaves it out. */
 double ref_force_softening(double r, double b) { return (double)force_softening((REAL)r, (REAL)b); }
+#endif
 
 #ifdef PERIODIC
 /* Builds the T^3 Ewald correction table exactly as main.cc:467-470 does:

@@ -177,16 +177,41 @@ class Engine:
         tab = np.ascontiguousarray(tab, dtype=np.float64)
         self._check(self.lib.steps_gpu_set_radial_table(int(tab.size), _d(tab)))
 
+    # batched ensembles
+    def batch_set(self, xs, ms, epss):
+        """Registers independent realisations (lists of x[n_k,3], m[n_k], eps[n_k])."""
+        self._batch = [(np.ascontiguousarray(x, dtype=np.float64), np.ascontiguousarray(m, dtype=np.float64),
+                        np.ascontiguousarray(e, dtype=np.float64)) for x, m, e in zip(xs, ms, epss)]
+        k = len(self._batch)
+        n = (C.c_int * k)(*[int(m.size) for _, m, _ in self._batch])
+        px = (_dp * k)(*[_d(x) for x, _, _ in self._batch])
+        pm = (_dp * k)(*[_d(m) for _, m, _ in self._batch])
+        pe = (_dp * k)(*[_d(e) for _, _, e in self._batch])
+        self._check(self.lib.steps_gpu_batch_set(k, n, px, pm, pe))
+
+    def batch_run(self, p: Params, precision, nsteps, h, graph=True):
+        self._check(self.lib.steps_gpu_batch_run(C.byref(p), int(precision), int(nsteps), float(h), int(bool(graph))))
+
+    def batch_get(self, k):
+        n = self._batch[k][1].size
+        x = np.empty((n, 3)); v = np.empty((n, 3)); F = np.empty((n, 3))
+        self._check(self.lib.steps_gpu_batch_get(int(k), _d(x), _d(v), _d(F)))
+        return x, v, F
+
     # tuning / instrumentation
     def set_tuning(self, threads, ipt, jsplit=0):
         self._check(self.lib.steps_gpu_set_tuning(int(threads), int(ipt), int(jsplit)))
 
     def autotune(self, p: Params, id_min=0, id_max=None):
-        out = (C.c_int * 2)()
+        """Returns (threads, ipt, variant) of the fastest mixed-precision kernel."""
+        out = (C.c_int * 3)()
         if id_max is None:
             id_max = self.n - 1
         self._check(self.lib.steps_gpu_autotune(C.byref(p), int(id_min), int(id_max), out))
-        return int(out[0]), int(out[1])
+        return int(out[0]), int(out[1]), int(out[2])
+
+    def set_variant(self, variant: int):
+        self._check(self.lib.steps_gpu_set_kernel_variant(int(variant)))
 
     def launch_count(self) -> int:
         return int(self.lib.steps_gpu_launch_count())

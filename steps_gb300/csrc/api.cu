@@ -149,7 +149,8 @@ void compute_forces(const steps_params *p, int precision, int id_min, int id_max
     if (precision == STEPS_FP64)
         forces_fp64(kp, tb, c.x.as<double>(), c.n, id_min, ni, F);
     else
-        forces_mixed(kp, tb, c.x.as<double>(), c.n, id_min, ni, F, reuse_order);
+        forces_mixed(kp, tb, c.x.as<double>(), c.m64.as<double>(), c.eps64.as<double>(), c.n, id_min, ni, F,
+                     reuse_order);
     c.F_lo = id_min;
     c.F_ni = ni;
     c.F_valid = id_min == 0 && ni == c.n;
@@ -215,12 +216,12 @@ int steps_gpu_shutdown(void)
         cudaStreamSynchronize(c.stream);
         batch_release();
         DevBuf *bufs[] = {&c.m64, &c.eps64, &c.x, &c.v, &c.F, &c.pack64, &c.partial, &c.bbox, &c.counter,
-                          &c.status, &c.flush, &c.peaks, &c.t3, &c.t3f, &c.s1r2, &c.radial};
+                          &c.status, &c.flush, &c.peaks, &c.t3, &c.t3f, &c.s1r2, &c.s1f, &c.radial};
         for (DevBuf *b : bufs) b->release();
         TileSet *ts[] = {&c.tj, &c.ti};
         for (TileSet *t : ts) {
             for (int k = 0; k < 2; k++) { t->keys[k].release(); t->vals[k].release(); }
-            t->hist.release(); t->pack.release(); t->eps.release(); t->meta.release(); t->idx.release(); t->resid.release();
+            t->hist.release(); t->pack.release(); t->eps.release(); t->meta.release(); t->idx.release(); t->resid.release(); t->soa.release();
             *t = TileSet();
         }
         for (auto &e : c.marks) cudaEventDestroy(e);
@@ -374,6 +375,7 @@ int steps_gpu_set_table_s1r2(int nrho, int nz, const double *table)
         STEPS_CUDA(cudaStreamSynchronize(c.stream));
         c.nrho = nrho;
         c.nz = nz;
+        c.s1r2_version++;
     });
 }
 
@@ -425,11 +427,14 @@ int steps_gpu_autotune(const steps_params *p, int id_min, int id_max, int *out)
         float best = 1e30f;
         Shape bestS = keep;
         KParams kp = derive_params(p);
+        const int nvar = kp.topology == STEPS_R3 ? 2 : 1;
+        for (int v = 0; v < nvar; v++)
         for (auto &s : shapes) {
             if (!shape_supported_for(kp, s[0], s[1])) continue;
             c.shape.threads = s[0];
             c.shape.ipt = s[1];
             c.shape.jsplit = 0;
+            c.shape.variant = v;
             compute_forces(p, STEPS_MIXED, id_min, id_max, false);  // warm
             compute_forces(p, STEPS_MIXED, id_min, id_max, true);
             STEPS_CUDA(cudaEventSynchronize(c.phase[2]));
@@ -439,7 +444,15 @@ int steps_gpu_autotune(const steps_params *p, int id_min, int id_max, int *out)
         }
         c.shape = bestS;
         c.shape_fixed = true;
-        if (out) { out[0] = bestS.threads; out[1] = bestS.ipt; }
+        if (out) { out[0] = bestS.threads; out[1] = bestS.ipt; out[2] = bestS.variant; }
+    });
+}
+
+int steps_gpu_set_kernel_variant(int variant)
+{
+    return guarded([&] {
+        if (variant != 0 && variant != 1) fail(STEPS_E_ARG, "kernel variant must be 0 (scalar) or 1 (packed FP32x2)");
+        g_ctx.shape.variant = variant;
     });
 }
 

@@ -1,32 +1,439 @@
-// Batched ensembles of independent R^3 realisations (placeholder until the
-// persistent work-queue kernel lands; every entry point reports STEPS_E_STATE).
+// Batched ensembles: many independent compactified R^3 realisations of uneven
+// N, advanced together (one force evaluation + fixed-dt KDK steps).
+//
+// Layout: all realisations' particles are concatenated (positions,
+// velocities, forces in caller order, realisation k at offset off[k]). One
+// radix sort orders every particle by (realisation, Morton key in that
+// realisation's own box), so each realisation occupies a contiguous range of
+// the sorted order; tiles never straddle two realisations (each realisation
+// is padded to a whole number of tiles).
+//
+// Work: a host-built list of items (i tile, j tile range, partial slot)
+// covering, for every realisation, its i tiles x j chunks; ordered by
+// realisation size, largest first, so the persistent kernel's atomic queue
+// schedules longest-processing-time first. The pair kernel is the packed
+// FP32x2 R^3 kernel in work-list mode; partial sums go to per-item slots and
+// a reduction adds each i tile's slots in order (deterministic).
+//
+// graph = 1: the whole run -- one force evaluation, then per step kick+drift,
+// re-order, re-tile, force, kick -- is captured once into a CUDA graph and
+// replayed; the tile shape is chosen by timing candidate shapes first.
+// graph = 0: the same work as `count` separate single-realisation force calls
+// (and KDK kernels) per phase, for comparison.
+#include <algorithm>
+#include <numeric>
+#include <vector>
+
 #include "common.cuh"
 #include "context.cuh"
+#include "mixed.cuh"
 
 namespace steps {
-void batch_release() {}
+
+struct Batch {
+    int count = 0;
+    std::vector<int> n, off;  // particles and their offset per realisation
+    int ntot = 0;
+    DevBuf x, v, F, m64, eps64;
+    DevBuf rel;                   // uint16 realisation of each particle (caller order)
+    DevBuf bbox;                  // 6 ordered-bit u64 per realisation
+    TileSet ts;                   // sort buffers + tile arrays over the padded batch
+    DevBuf tdesc;                 // int2 per tile: sorted start, count
+    DevBuf items;                 // int4 work list
+    DevBuf tslot;                 // int2 per tile: first partial slot, number of slots
+    DevBuf part, counter, err;
+    int T = 0, ntiles = 0, nitems = 0, threads = 0, ipt = 0, grid = 0;
+    bool tuned = false;
+    cudaGraphExec_t exec = nullptr;
+    int graph_steps = -1;
+    double graph_h = 0.0;
+};
+
+namespace {
+
+__global__ void k_batch_bbox(const double *__restrict__ x, const uint16_t *__restrict__ rel, int n,
+                             unsigned long long *bb)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int k = rel[i];
+        for (int c = 0; c < 3; c++) {
+            const double v = x[3 * (size_t)i + c];
+            atomicMin(&bb[6 * k + c], ordered_bits(v));
+            atomicMax(&bb[6 * k + 3 + c], ordered_bits(v));
+        }
+    }
+}
+
+__global__ void k_batch_bbox_init(unsigned long long *bb, int count)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < 6 * count) bb[t] = (t % 6) < 3 ? ~0ull : 0ull;
+}
+
+// Key = realisation index (13 bits) above a 51-bit Morton key (17 bits per
+// axis) of the particle's position in its realisation's own bounding box.
+__global__ void k_batch_keys(const double *__restrict__ x, const uint16_t *__restrict__ rel, int n,
+                             const unsigned long long *__restrict__ bb, unsigned long long *keys, uint32_t *vals)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int k = rel[i];
+    const double cells = (double)(1u << 17);
+    unsigned long long key = 0;
+    for (int c = 0; c < 3; c++) {
+        const double lo = from_ordered_bits(bb[6 * k + c]), hi = from_ordered_bits(bb[6 * k + 3 + c]);
+        const double span = hi - lo;
+        const double u = span > 0 ? (x[3 * (size_t)i + c] - lo) / span * cells : 0.0;
+        long long q = (long long)u;
+        q = q < 0 ? 0 : (q >= (long long)cells ? (long long)cells - 1 : q);
+        key |= spread3((unsigned long long)q) << c;
+    }
+    keys[i] = key | ((unsigned long long)k << 51);
+    vals[i] = (uint32_t)i;
+}
+
+// Sum each i's slots in order and scatter to caller order.
+__global__ void k_batch_reduce(const double *__restrict__ part, const int2 *__restrict__ tslot,
+                               const uint32_t *__restrict__ idx, int npad, int T, double *__restrict__ F)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= npad) return;
+    const uint32_t o = idx[q];
+    if (o == PAD_J) return;
+    const int t = q / T, e = q - t * T;
+    const int2 s = tslot[t];
+    double f[3] = {0, 0, 0};
+    for (int k = 0; k < s.y; k++)
+        for (int c = 0; c < 3; c++) f[c] += part[((size_t)(s.x + k) * T + e) * 3 + c];
+    for (int c = 0; c < 3; c++) F[3 * (size_t)o + c] = f[c];
+}
+
+Batch *B() { return ctx().batch; }
+
+// Tile descriptors and the work list for tile size T (host side, once per shape).
+void plan(Batch &b, int threads, int ipt)
+{
+    Ctx &c = ctx();
+    const int T = threads * ipt;
+    std::vector<int> tstart(b.count), nt(b.count);
+    std::vector<int2> desc;
+    for (int k = 0; k < b.count; k++) {
+        nt[k] = div_up(b.n[k], T);
+        tstart[k] = (int)desc.size();
+        for (int t = 0; t < nt[k]; t++) desc.push_back(make_int2(b.off[k] + t * T, std::min(T, b.n[k] - t * T)));
+    }
+    b.ntiles = (int)desc.size();
+    // Items: per realisation i tiles x j chunks of at most 256 tiles; largest realisations first.
+    std::vector<int> order(b.count);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int d) { return b.n[a] > b.n[d]; });
+    std::vector<int4> items;
+    std::vector<int2> tslot(b.ntiles);
+    for (int k : order) {
+        const int S = div_up(nt[k], 256);
+        const int per = div_up(nt[k], S);
+        for (int I = 0; I < nt[k]; I++) {
+            const int gI = tstart[k] + I;
+            tslot[gI] = make_int2((int)items.size(), 0);
+            for (int s = 0; s < S; s++) {
+                const int J0 = tstart[k] + s * per, J1 = std::min(tstart[k] + nt[k], J0 + per);
+                if (J0 >= J1) continue;
+                items.push_back(make_int4(gI, J0, J1, (int)items.size()));
+                tslot[gI].y++;
+            }
+        }
+    }
+    b.nitems = (int)items.size();
+    const size_t padded = (size_t)b.ntiles * T;
+    STEPS_CUDA(cudaMemcpyAsync(b.tdesc.ensure<int2>(desc.size()), desc.data(), desc.size() * sizeof(int2),
+                               cudaMemcpyHostToDevice, c.stream));
+    STEPS_CUDA(cudaMemcpyAsync(b.items.ensure<int4>(items.size()), items.data(), items.size() * sizeof(int4),
+                               cudaMemcpyHostToDevice, c.stream));
+    STEPS_CUDA(cudaMemcpyAsync(b.tslot.ensure<int2>(tslot.size()), tslot.data(), tslot.size() * sizeof(int2),
+                               cudaMemcpyHostToDevice, c.stream));
+    b.ts.pack.ensure<float4>(padded);
+    b.ts.eps.ensure<float>(padded);
+    b.ts.meta.ensure<float4>(2 * (size_t)b.ntiles);
+    b.ts.idx.ensure<uint32_t>(padded);
+    b.ts.resid.ensure<float4>(padded);
+    b.ts.soa.ensure<float4>(padded);
+    b.part.ensure<double>((size_t)b.nitems * T * 3);
+    b.T = T;
+    b.threads = threads;
+    b.ipt = ipt;
+    mixed::KernelFn fn = r3x2_kernel(threads, ipt, true);
+    if (!fn) fail(STEPS_E_ARG, "batch: unsupported kernel shape");
+    int occ = 0;
+    STEPS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, threads, 0));
+    b.grid = std::min(c.nsm * std::max(occ, 1), b.nitems);
+    STEPS_CUDA(cudaStreamSynchronize(c.stream));
+}
+
+// One batched force evaluation on the resident positions (stream-ordered; no
+// host synchronisation, so it can be captured into a graph).
+void batch_forces(Batch &b)
+{
+    Ctx &c = ctx();
+    cudaStream_t st = c.stream;
+    unsigned long long *bb = b.bbox.as<unsigned long long>();
+    k_batch_bbox_init<<<div_up(6 * b.count, 256), 256, 0, st>>>(bb, b.count);
+    note_launch("k_batch_bbox_init");
+    k_batch_bbox<<<std::min(div_up(b.ntot, 256), 4 * c.nsm * 8), 256, 0, st>>>(b.x.as<double>(), b.rel.as<uint16_t>(),
+                                                                            b.ntot, bb);
+    note_launch("k_batch_bbox");
+    k_batch_keys<<<div_up(b.ntot, 256), 256, 0, st>>>(b.x.as<double>(), b.rel.as<uint16_t>(), b.ntot, bb,
+                                                      b.ts.keys[0].as<unsigned long long>(),
+                                                      b.ts.vals[0].as<uint32_t>());
+    note_launch("k_batch_keys");
+    sort_pairs(b.ts, b.ntot, st);
+    tile_build_range(b.x.as<double>(), b.m64.as<double>(), b.eps64.as<double>(), b.ts.perm(), b.ntot, b.T,
+                     b.ts.pack.as<float4>(), b.ts.eps.as<float>(), b.ts.meta.as<float4>(), b.ts.idx.as<uint32_t>(),
+                     PAD_J, b.ts.resid.as<float4>(), b.ts.soa.as<float>(), b.tdesc.as<int2>(), b.ntiles, st);
+
+    mixed::MixedArgs a{};
+    a.jpack = a.ipack = b.ts.pack.as<float4>();
+    a.jeps = a.ieps = b.ts.eps.as<float>();
+    a.jmeta = a.imeta = b.ts.meta.as<float4>();
+    a.jidx = a.iidx = b.ts.idx.as<uint32_t>();
+    a.jres = a.ilo = b.ts.resid.as<float4>();
+    a.jsoa = b.ts.soa.as<float>();
+    a.njt = a.nit = b.ntiles;
+    a.nitems = b.nitems;
+    a.items = b.items.as<int4>();
+    a.counter = b.counter.as<unsigned>();
+    a.part = b.part.as<double>();
+    mixed::KernelFn fn = r3x2_kernel(b.threads, b.ipt, true);
+    STEPS_CUDA(cudaMemsetAsync(a.counter, 0, sizeof(unsigned), st));
+    fn<<<b.grid, b.threads, 0, st>>>(a);
+    note_launch("k_pair_r3x2(list)");
+    k_batch_reduce<<<div_up(b.ntiles * b.T, 256), 256, 0, st>>>(b.part.as<double>(), b.tslot.as<int2>(),
+                                                                b.ts.idx.as<uint32_t>(), b.ntiles * b.T, b.T,
+                                                                b.F.as<double>());
+    note_launch("k_batch_reduce");
+}
+
+void batch_steps(Batch &b, int nsteps, double h)
+{
+    Ctx &c = ctx();
+    batch_forces(b);
+    for (int s = 0; s < nsteps; s++) {
+        kdk_kick_drift(b.x.as<double>(), b.v.as<double>(), b.F.as<double>(), b.ntot, h, 1.0, 1.0, 0.0, 0, 0.0,
+                       c.stream);
+        batch_forces(b);
+        kdk_kick_err(b.v.as<double>(), b.F.as<double>(), b.m64.as<double>(), b.ntot, h, 1.0, 1.0, 0.0, 1.0,
+                     b.err.as<double>(), c.stream, false);
+    }
+}
+
+// Per-realisation path: the same work as `count` separate force calls.
+void plain_steps(Batch &b, const KParams &kp, int precision, int nsteps, double h)
+{
+    Ctx &c = ctx();
+    Tables tb{};
+    auto force = [&](int k) {
+        const size_t o = (size_t)b.off[k];
+        double *x = b.x.as<double>() + 3 * o, *F = b.F.as<double>() + 3 * o;
+        const double *m = b.m64.as<double>() + o, *e = b.eps64.as<double>() + o;
+        if (precision == STEPS_FP64) fail(STEPS_E_ARG, "batch: FP64 ensembles are not supported");
+        forces_mixed(kp, tb, x, m, e, b.n[k], 0, b.n[k], F, false);
+    };
+    for (int k = 0; k < b.count; k++) force(k);
+    for (int s = 0; s < nsteps; s++) {
+        for (int k = 0; k < b.count; k++) {
+            const size_t o = (size_t)b.off[k];
+            kdk_kick_drift(b.x.as<double>() + 3 * o, b.v.as<double>() + 3 * o, b.F.as<double>() + 3 * o, b.n[k], h,
+                           1.0, 1.0, 0.0, 0, 0.0, c.stream);
+            force(k);
+            kdk_kick_err(b.v.as<double>() + 3 * o, b.F.as<double>() + 3 * o, b.m64.as<double>() + o, b.n[k], h, 1.0,
+                         1.0, 0.0, 1.0, b.err.as<double>(), c.stream, false);
+        }
+    }
+}
+
+void release_graph(Batch &b)
+{
+    if (b.exec) cudaGraphExecDestroy(b.exec);
+    b.exec = nullptr;
+    b.graph_steps = -1;
+}
+
+}  // namespace
+
+void batch_release()
+{
+    Ctx &c = ctx();
+    Batch *b = c.batch;
+    if (!b) return;
+    release_graph(*b);
+    DevBuf *bufs[] = {&b->x, &b->v, &b->F, &b->m64, &b->eps64, &b->rel, &b->bbox, &b->tdesc, &b->items, &b->tslot,
+                      &b->part, &b->counter, &b->err, &b->ts.keys[0], &b->ts.keys[1], &b->ts.vals[0], &b->ts.vals[1],
+                      &b->ts.hist, &b->ts.pack, &b->ts.eps, &b->ts.meta, &b->ts.idx, &b->ts.resid, &b->ts.soa};
+    for (DevBuf *d : bufs) d->release();
+    delete b;
+    c.batch = nullptr;
+}
+
 }  // namespace steps
 
 using namespace steps;
 
 extern "C" {
 
-int steps_gpu_batch_set(int, const int *, const double *const *, const double *const *, const double *const *)
+int steps_gpu_batch_set(int count, const int *n, const double *const *x, const double *const *m,
+                        const double *const *eps)
 {
-    return run_guarded([](void *) { fail(STEPS_E_STATE, "batched ensembles are not available in this build"); },
-                       nullptr);
+    struct A {
+        int count;
+        const int *n;
+        const double *const *x, *const *m, *const *eps;
+    } args{count, n, x, m, eps};
+    return run_guarded(
+        [](void *vp) {
+            A &a = *static_cast<A *>(vp);
+            require_init();
+            Ctx &c = ctx();
+            if (a.count < 1 || a.count > 8191 || !a.n || !a.x || !a.m || !a.eps)
+                fail(STEPS_E_ARG, "batch_set: count in [1, 8191] and non-NULL arrays required");
+            long long tot = 0;
+            for (int k = 0; k < a.count; k++) {
+                if (a.n[k] < 1 || !a.x[k] || !a.m[k] || !a.eps[k]) fail(STEPS_E_ARG, "batch_set: empty realisation");
+                tot += a.n[k];
+            }
+            if (tot > (1LL << 30)) fail(STEPS_E_ARG, "batch_set: too many particles");
+            batch_release();
+            c.batch = new Batch();
+            Batch &b = *c.batch;
+            b.count = a.count;
+            b.n.assign(a.n, a.n + a.count);
+            b.off.resize(a.count);
+            int o = 0;
+            for (int k = 0; k < a.count; k++) { b.off[k] = o; o += a.n[k]; }
+            b.ntot = o;
+            std::vector<uint16_t> rel(b.ntot);
+            for (int k = 0; k < a.count; k++) std::fill(rel.begin() + b.off[k], rel.begin() + b.off[k] + b.n[k], k);
+            double *dx = b.x.ensure<double>(3 * (size_t)b.ntot);
+            double *dm = b.m64.ensure<double>(b.ntot), *de = b.eps64.ensure<double>(b.ntot);
+            for (int k = 0; k < a.count; k++) {
+                const size_t off = (size_t)b.off[k];
+                STEPS_CUDA(cudaMemcpyAsync(dx + 3 * off, a.x[k], 3 * sizeof(double) * a.n[k], cudaMemcpyHostToDevice,
+                                           c.stream));
+                STEPS_CUDA(cudaMemcpyAsync(dm + off, a.m[k], sizeof(double) * a.n[k], cudaMemcpyHostToDevice,
+                                           c.stream));
+                STEPS_CUDA(cudaMemcpyAsync(de + off, a.eps[k], sizeof(double) * a.n[k], cudaMemcpyHostToDevice,
+                                           c.stream));
+            }
+            STEPS_CUDA(cudaMemsetAsync(b.v.ensure<double>(3 * (size_t)b.ntot), 0, 3 * sizeof(double) * b.ntot,
+                                       c.stream));
+            b.F.ensure<double>(3 * (size_t)b.ntot);
+            STEPS_CUDA(cudaMemcpyAsync(b.rel.ensure<uint16_t>(b.ntot), rel.data(), sizeof(uint16_t) * b.ntot,
+                                       cudaMemcpyHostToDevice, c.stream));
+            b.bbox.ensure<unsigned long long>(6 * (size_t)a.count);
+            for (int k = 0; k < 2; k++) {
+                b.ts.keys[k].ensure<unsigned long long>(b.ntot);
+                b.ts.vals[k].ensure<uint32_t>(b.ntot);
+            }
+            b.counter.ensure<unsigned>(4);
+            b.err.ensure<double>(4);
+            STEPS_CUDA(cudaStreamSynchronize(c.stream));
+        },
+        &args);
 }
 
-int steps_gpu_batch_run(const steps_params *, int, int, double, int)
+int steps_gpu_batch_run(const steps_params *p, int precision, int nsteps, double h, int graph)
 {
-    return run_guarded([](void *) { fail(STEPS_E_STATE, "batched ensembles are not available in this build"); },
-                       nullptr);
+    struct A {
+        const steps_params *p;
+        int precision, nsteps;
+        double h;
+        int graph;
+    } args{p, precision, nsteps, h, graph};
+    return run_guarded(
+        [](void *vp) {
+            A &a = *static_cast<A *>(vp);
+            require_init();
+            Ctx &c = ctx();
+            Batch *bp = c.batch;
+            if (!bp) fail(STEPS_E_STATE, "no batch: call steps_gpu_batch_set first");
+            Batch &b = *bp;
+            KParams kp = derive_params(a.p);
+            if (kp.topology != STEPS_R3 || kp.comoving_bg != 0)
+                fail(STEPS_E_ARG, "batch: non-cosmological R^3 realisations only");
+            if (a.nsteps < 0) fail(STEPS_E_ARG, "batch: nsteps must be >= 0");
+            if (!a.graph) {
+                plain_steps(b, kp, a.precision, a.nsteps, a.h);
+                STEPS_CUDA(cudaStreamSynchronize(c.stream));
+                return;
+            }
+            if (a.precision != STEPS_MIXED) fail(STEPS_E_ARG, "batch graph: mixed precision only");
+            if (!b.tuned) {
+                // Time one batched force per candidate shape, keep the fastest.
+                static const int shapes[][2] = {{128, 2}, {64, 4}, {128, 1}, {256, 1}, {128, 4}, {256, 2}};
+                float best = 1e30f;
+                int bt = 128, bi = 2;
+                for (auto &s : shapes) {
+                    plan(b, s[0], s[1]);
+                    batch_forces(b);  // warm
+                    STEPS_CUDA(cudaEventRecord(c.marks[12], c.stream));
+                    batch_forces(b);
+                    STEPS_CUDA(cudaEventRecord(c.marks[13], c.stream));
+                    STEPS_CUDA(cudaEventSynchronize(c.marks[13]));
+                    float ms = 0;
+                    STEPS_CUDA(cudaEventElapsedTime(&ms, c.marks[12], c.marks[13]));
+                    if (ms < best) { best = ms; bt = s[0]; bi = s[1]; }
+                }
+                plan(b, bt, bi);
+                b.tuned = true;
+                release_graph(b);
+            }
+            if (!b.exec || b.graph_steps != a.nsteps || b.graph_h != a.h) {
+                release_graph(b);
+                batch_forces(b);  // sizes every buffer before capture
+                STEPS_CUDA(cudaStreamSynchronize(c.stream));
+                cudaGraph_t g;
+                STEPS_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+                try {
+                    batch_steps(b, a.nsteps, a.h);
+                } catch (...) {
+                    cudaGraph_t dummy;
+                    cudaStreamEndCapture(c.stream, &dummy);
+                    if (dummy) cudaGraphDestroy(dummy);
+                    throw;
+                }
+                STEPS_CUDA(cudaStreamEndCapture(c.stream, &g));
+                cudaError_t e = cudaGraphInstantiate(&b.exec, g, 0);
+                cudaGraphDestroy(g);
+                STEPS_CUDA(e);
+                b.graph_steps = a.nsteps;
+                b.graph_h = a.h;
+            }
+            STEPS_CUDA(cudaGraphLaunch(b.exec, c.stream));
+            c.launches += 1;
+            STEPS_CUDA(cudaStreamSynchronize(c.stream));
+        },
+        &args);
 }
 
-int steps_gpu_batch_get(int, double *, double *, double *)
+int steps_gpu_batch_get(int k, double *x, double *v, double *F)
 {
-    return run_guarded([](void *) { fail(STEPS_E_STATE, "batched ensembles are not available in this build"); },
-                       nullptr);
+    struct A {
+        int k;
+        double *x, *v, *F;
+    } args{k, x, v, F};
+    return run_guarded(
+        [](void *vp) {
+            A &a = *static_cast<A *>(vp);
+            require_init();
+            Ctx &c = ctx();
+            Batch *b = c.batch;
+            if (!b) fail(STEPS_E_STATE, "no batch: call steps_gpu_batch_set first");
+            if (a.k < 0 || a.k >= b->count) fail(STEPS_E_ARG, "batch_get: no such realisation");
+            const size_t o = 3 * (size_t)b->off[a.k], bytes = 3 * sizeof(double) * b->n[a.k];
+            if (a.x) STEPS_CUDA(cudaMemcpyAsync(a.x, b->x.as<double>() + o, bytes, cudaMemcpyDeviceToHost, c.stream));
+            if (a.v) STEPS_CUDA(cudaMemcpyAsync(a.v, b->v.as<double>() + o, bytes, cudaMemcpyDeviceToHost, c.stream));
+            if (a.F) STEPS_CUDA(cudaMemcpyAsync(a.F, b->F.as<double>() + o, bytes, cudaMemcpyDeviceToHost, c.stream));
+            STEPS_CUDA(cudaStreamSynchronize(c.stream));
+        },
+        &args);
 }
 
 }  // extern "C"

@@ -74,6 +74,7 @@ struct TileSet {
     DevBuf pack, eps, meta;
     DevBuf idx;  // idx[q] = original index of curve position q; padding holds pad_id
     DevBuf resid;  // resid[q] = (x - c) - pack[q].xyz, the FP32 residual of the offset
+    DevBuf soa;    // tile-blocked SoA copy of pack: X[T], Y[T], Z[T], M[T] per tile
     int perm_sel = 0;  // vals[perm_sel] holds curve position -> original index
     bool ordered = false;
     const uint32_t *perm() const { return vals[perm_sel].as<uint32_t>(); }
@@ -84,6 +85,7 @@ struct Shape {
     int threads = 128;
     int ipt = 2;
     int jsplit = 0;
+    int variant = 0;  // R^3: 0 scalar FP32 pair loop, 1 packed FP32x2 pair loop
 };
 
 // ------------------------------------------------------------- utilities --
@@ -94,6 +96,33 @@ inline __host__ __device__ int div_up(int a, int b) { return (a + b - 1) / b; }
 void note_launch(const char *name);
 
 // ---------------------------------------------------- device math helpers --
+
+// Order-preserving integer image of a double (atomic min/max of bounding boxes).
+__device__ __forceinline__ unsigned long long ordered_bits(double d)
+{
+    unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+}
+
+__device__ __forceinline__ double from_ordered_bits(unsigned long long u)
+{
+    unsigned long long b = (u & 0x8000000000000000ull) ? (u & 0x7fffffffffffffffull) : ~u;
+    return __longlong_as_double((long long)b);
+}
+
+__device__ __forceinline__ unsigned long long spread3(unsigned long long v)
+{
+    // Spread the low 21 bits of v to every third bit.
+    v &= 0x1fffffull;
+    v = (v | (v << 32)) & 0x1f00000000ffffull;
+    v = (v | (v << 16)) & 0x1f0000ff0000ffull;
+    v = (v | (v << 8)) & 0x100f00f00f00f00full;
+    v = (v | (v << 4)) & 0x10c30c30c30c30c3ull;
+    v = (v | (v << 2)) & 0x1249249249249249ull;
+    return v;
+}
+
+
 
 // MUFU reciprocal square root, approximate (relative error < 2^-22), FTZ.
 __device__ __forceinline__ float rsqrt_mufu(float x)

@@ -36,6 +36,9 @@ struct Ctx {
     long long t3f_version = -1;
     DevBuf s1r2;
     int nrho = 0, nz = 0;
+    long long s1r2_version = 0;
+    DevBuf s1f;  // FP32 float2 copy for the mixed kernel
+    long long s1f_version = -1;
     DevBuf radial;
     int radial_size = 0;
 
@@ -63,16 +66,16 @@ void sort_pairs(TileSet &ts, int n, cudaStream_t st);
 void batch_keys(const double *x, int lo, int count, unsigned long long prefix, unsigned long long *keys, uint32_t *vals,
                 unsigned long long *bbox_scratch, cudaStream_t st);
 void tile_build_range(const double *x, const double *m64, const double *eps64, const uint32_t *perm, int count, int T,
-                      float4 *pack, float *epsf, float4 *meta, uint32_t *idx, uint32_t pad_id, float4 *lo,
-                      cudaStream_t st);
+                      float4 *pack, float *epsf, float4 *meta, uint32_t *idx, uint32_t pad_id, float4 *lo, float *soa,
+                      const int2 *tdesc, int ntiles, cudaStream_t st);
 
 // pair_fp64.cu: FP64 forces of i in [id_min, id_min+ni) into F[3*ni] (with background).
 void forces_fp64(const KParams &kp, const Tables &tb, const double *x, int n, int id_min, int ni, double *F);
 
 // pair_mixed.cu
 struct MixedLaunch;
-void forces_mixed(const KParams &kp, const Tables &tb, const double *x, int n, int id_min, int ni, double *F,
-                  bool reuse_order);
+void forces_mixed(const KParams &kp, const Tables &tb, const double *x, const double *m64, const double *eps64,
+                  int n, int id_min, int ni, double *F, bool reuse_order);
 bool shape_supported(int threads, int ipt);
 bool shape_supported_for(const KParams &kp, int threads, int ipt);
 

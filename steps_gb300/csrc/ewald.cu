@@ -317,6 +317,7 @@ int steps_gpu_build_table_s1r2(int nrho, int nz, double rho_max, double lz, doub
             STEPS_CUDA(cudaStreamSynchronize(c.stream));
             c.nrho = a.nrho;
             c.nz = a.nz;
+            c.s1r2_version++;
         },
         &a);
 }

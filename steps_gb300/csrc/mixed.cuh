@@ -14,6 +14,8 @@ struct MixedArgs {
     const float *jeps;
     const float4 *jmeta;
     const uint32_t *jidx;
+    const float4 *jres;  // FP32 residuals of the j offsets (double-float near path)
+    const float *jsoa;   // tile-blocked SoA copy of jpack (packed-FP32 kernel)
     int njt;
     const float4 *ipack;
     const float *ieps;
@@ -24,9 +26,11 @@ struct MixedArgs {
     int S, tpc;  // j chunks per i tile, j tiles per chunk
     int nitems;
     unsigned *counter;
+    const int4 *items;  // work list (batches): i tile, j tile begin, j tile end, partial slot
     double *part;       // [S][nit*T][3]
     size_t part_stride; // nit*T*3
     float L, halfL, cutL;
+    float cut_tol;      // |dz + mL| this close to cutL is re-decided on an exact dz
     int emax;
     int nearest;        // S1R2 IS_PERIODIC == 1: nearest image along z only
     // T^3 Ewald table (FP32 copy, one float4 per cell) and its geometry
@@ -34,6 +38,10 @@ struct MixedArgs {
     int ng;
     float ih, u0;       // continuous cell index u(d) = d * ih + u0, ih = ng / L, u0 = ng/2 - 1/2
     int wcap;           // cells of the shared-memory table window
+    // S1xR2 (rho, z) correction table (FP32 float2 copy) and its geometry
+    const float2 *s1tab;
+    int nrho, nz;
+    float irho, iz, rho_max;  // 1 / drho, nz / L_z
 };
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
@@ -51,7 +59,8 @@ template <int N>
 __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
 
 template <int BLOCK, int IPT>
-__device__ __forceinline__ void stage_tile(const MixedArgs &a, int J, float4 *sp, float *se, uint32_t *sid)
+__device__ __forceinline__ void stage_tile(const MixedArgs &a, int J, float4 *sp, float *se, uint32_t *sid,
+                                           float4 *sres)
 {
     constexpr int T = BLOCK * IPT;
 #pragma unroll
@@ -61,6 +70,7 @@ __device__ __forceinline__ void stage_tile(const MixedArgs &a, int J, float4 *sp
         cp_async16(sp + e, a.jpack + q);
         cp_async4(se + e, a.jeps + q);
         cp_async4(sid + e, a.jidx + q);
+        cp_async16(sres + e, a.jres + q);
     }
     cp_commit();
 }
@@ -74,6 +84,25 @@ __device__ __forceinline__ float two_diff(float a, float b, float &e)
     return s;
 }
 
+// The FP32 tile offsets carry ~6e-8 of the tile-pair scale |d_O| + h_I + h_J;
+// where that scale exceeds 30x the box gap, a pair can be close enough for
+// this to matter, and the block takes the double-float (full) path.
+__device__ __forceinline__ bool coarse_for_gap(float dOx, float dOy, float dOz, float4 hI, float4 hJ, float g2)
+{
+    const float s = sqrtf(dOx * dOx + dOy * dOy + dOz * dOz) + sqrtf(hI.x * hI.x + hI.y * hI.y + hI.z * hI.z) +
+                    sqrtf(hJ.x * hJ.x + hJ.y * hJ.y + hJ.z * hJ.z);
+    return s * s > 900.0f * g2;
+}
+
+// i particle k in J's frame as an unevaluated sum ph + pl: ph = fl(x_hi - dO),
+// pl = its rounding error (exact) - eO + x_lo.
+__device__ __forceinline__ void frame_split(float xh, float xl, float dO, float eO, float &ph, float &pl)
+{
+    float e;
+    ph = two_diff(xh, dO, e);
+    pl = (e - eO) + xl;
+}
+
 // Lower bound of |d| over the separations of two boxes along one axis.
 __device__ __forceinline__ float axis_gap(float dO, float hI, float hJ) { return fmaxf(fabsf(dO) - hI - hJ, 0.0f); }
 
@@ -85,5 +114,10 @@ using KernelFn = void (*)(MixedArgs);
 // table arguments (FP32 table copy, grid geometry).
 mixed::KernelFn t3_kernel(const KParams &kp, int threads, int ipt, size_t *dyn_smem);
 void t3_args(mixed::MixedArgs &a, const KParams &kp, const Tables &tb, cudaStream_t st);
+// pair_r3x2.cu: R^3 kernel on packed FP32 pairs.
+mixed::KernelFn r3x2_kernel(int threads, int ipt, bool list = false);
+// S1xR2 with the (rho, z) table (IS_PERIODIC >= 2, no explicit images).
+mixed::KernelFn s1tab_kernel(const KParams &kp, int threads, int ipt);
+void s1tab_args(mixed::MixedArgs &a, const KParams &kp, const Tables &tb, cudaStream_t st);
 
 }  // namespace steps

@@ -20,18 +20,6 @@ constexpr int SORT_TILE = SORT_THREADS * SORT_ITEMS;
 constexpr int RADIX_BITS = 8;
 constexpr int RADIX = 1 << RADIX_BITS;
 
-__device__ __forceinline__ unsigned long long ordered_bits(double d)
-{
-    unsigned long long b = (unsigned long long)__double_as_longlong(d);
-    return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
-}
-
-__device__ __forceinline__ double from_ordered_bits(unsigned long long u)
-{
-    unsigned long long b = (u & 0x8000000000000000ull) ? (u & 0x7fffffffffffffffull) : ~u;
-    return __longlong_as_double((long long)b);
-}
-
 __global__ void k_bbox_init(unsigned long long *bb)
 {
     int t = threadIdx.x;
@@ -56,18 +44,6 @@ __global__ void k_bbox(const double *__restrict__ x, int lo, int count, unsigned
             atomicMin(&bb[k], ordered_bits(mn[k]));
             atomicMax(&bb[3 + k], ordered_bits(mx[k]));
         }
-}
-
-__device__ __forceinline__ unsigned long long spread3(unsigned long long v)
-{
-    // Spread the low 21 bits of v to every third bit.
-    v &= 0x1fffffull;
-    v = (v | (v << 32)) & 0x1f00000000ffffull;
-    v = (v | (v << 16)) & 0x1f0000ff0000ffull;
-    v = (v | (v << 8)) & 0x100f00f00f00f00full;
-    v = (v | (v << 4)) & 0x10c30c30c30c30c3ull;
-    v = (v | (v << 2)) & 0x1249249249249249ull;
-    return v;
 }
 
 // Keys for particles lo..lo+count-1; prefix (the realisation index of a batch)
@@ -196,17 +172,22 @@ __global__ void __launch_bounds__(TB_THREADS) k_tile_build(const double *__restr
                                                           const uint32_t *__restrict__ perm, int count, int T,
                                                           float4 *__restrict__ pack, float *__restrict__ epsf,
                                                           float4 *__restrict__ meta, uint32_t *__restrict__ idx,
-                                                          uint32_t pad_id, float4 *__restrict__ lo)
+                                                          uint32_t pad_id, float4 *__restrict__ lo,
+                                                          float *__restrict__ soa, const int2 *__restrict__ tdesc)
 {
     __shared__ double red[7][TB_THREADS / 32];
     __shared__ float s_c[3];
     int tile = blockIdx.x;
     int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    // Sorted positions of this tile's particles: [sbase, sbase + cnt). Without
+    // descriptors the tiles cut one sorted set; with them (batches) every
+    // tile names its own start and count.
+    const int sbase = tdesc ? tdesc[tile].x : tile * T;
+    const int cnt = tdesc ? tdesc[tile].y : min(T, count - tile * T);
     double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300}, em = 0.0;
     for (int e = t; e < T; e += TB_THREADS) {
-        int q = tile * T + e;
-        if (q < count) {
-            uint32_t o = perm[q];
+        if (e < cnt) {
+            uint32_t o = perm[sbase + e];
             for (int k = 0; k < 3; k++) {
                 double v = x[3 * (size_t)o + k];
                 mn[k] = fmin(mn[k], v);
@@ -244,13 +225,20 @@ __global__ void __launch_bounds__(TB_THREADS) k_tile_build(const double *__restr
     __syncthreads();
     double cx = s_c[0], cy = s_c[1], cz = s_c[2];
     for (int e = t; e < T; e += TB_THREADS) {
-        int q = tile * T + e;
-        if (q < count) {
-            uint32_t o = perm[q];
+        const int q = tile * T + e;
+        if (e < cnt) {
+            uint32_t o = perm[sbase + e];
             const double *p = x + 3 * (size_t)o;
             const double ox = p[0] - cx, oy = p[1] - cy, oz = p[2] - cz;
             const float hx = __double2float_rn(ox), hy = __double2float_rn(oy), hz = __double2float_rn(oz);
             pack[q] = make_float4(hx, hy, hz, __double2float_rn(m[o]));
+            if (soa) {  // tile-blocked SoA copy: X[T], Y[T], Z[T], M[T] per tile
+                float *b = soa + (size_t)tile * 4 * T;
+                b[e] = hx;
+                b[T + e] = hy;
+                b[2 * T + e] = hz;
+                b[3 * T + e] = __double2float_rn(m[o]);
+            }
             // What FP32 dropped from the offset: i particles carry it so that
             // their position in another tile's frame keeps full precision.
             if (lo)
@@ -260,6 +248,10 @@ __global__ void __launch_bounds__(TB_THREADS) k_tile_build(const double *__restr
             if (idx) idx[q] = o;
         } else {
             pack[q] = make_float4(0.f, 0.f, 0.f, 0.f);  // massless padding at the tile centre
+            if (soa) {
+                float *b = soa + (size_t)tile * 4 * T;
+                b[e] = b[T + e] = b[2 * T + e] = b[3 * T + e] = 0.f;
+            }
             if (lo) lo[q] = make_float4(0.f, 0.f, 0.f, 0.f);
             epsf[q] = 0.f;
             if (idx) idx[q] = pad_id;
@@ -321,9 +313,10 @@ void build_tiles(TileSet &ts, const double *x, const double *m64, const double *
     ts.meta.ensure<float4>(2 * (size_t)ts.ntiles);
     ts.idx.ensure<uint32_t>(padded);
     ts.resid.ensure<float4>(padded);
+    ts.soa.ensure<float4>(padded);
     k_tile_build<<<ts.ntiles, TB_THREADS, 0, st>>>(x, m64, eps64, ts.perm(), count, T, ts.pack.as<float4>(),
                                                    ts.eps.as<float>(), ts.meta.as<float4>(), ts.idx.as<uint32_t>(),
-                                                   pad_id, ts.resid.as<float4>());
+                                                   pad_id, ts.resid.as<float4>(), ts.soa.as<float>(), nullptr);
     note_launch("k_tile_build");
 }
 
@@ -342,11 +335,12 @@ void batch_keys(const double *x, int lo, int count, unsigned long long prefix, u
 }
 
 void tile_build_range(const double *x, const double *m64, const double *eps64, const uint32_t *perm, int count, int T,
-                      float4 *pack, float *epsf, float4 *meta, uint32_t *idx, uint32_t pad_id, float4 *lo,
-                      cudaStream_t st)
+                      float4 *pack, float *epsf, float4 *meta, uint32_t *idx, uint32_t pad_id, float4 *lo, float *soa,
+                      const int2 *tdesc, int ntiles, cudaStream_t st)
 {
-    int nt = div_up(count, T);
-    k_tile_build<<<nt, TB_THREADS, 0, st>>>(x, m64, eps64, perm, count, T, pack, epsf, meta, idx, pad_id, lo);
+    int nt = tdesc ? ntiles : div_up(count, T);
+    k_tile_build<<<nt, TB_THREADS, 0, st>>>(x, m64, eps64, perm, count, T, pack, epsf, meta, idx, pad_id, lo, soa,
+                                            tdesc);
     note_launch("k_tile_build");
 }
 

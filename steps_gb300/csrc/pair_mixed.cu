@@ -33,13 +33,14 @@ namespace {
 using namespace mixed;
 
 template <int KIND, int BLOCK, int IPT, int EMAX>
-__global__ void __launch_bounds__(BLOCK) k_pair_mixed(MixedArgs a)
+__global__ void __launch_bounds__(BLOCK, KIND == K_R3 && IPT == 1 ? 1024 / BLOCK : 1) k_pair_mixed(MixedArgs a)
 {
     constexpr int T = BLOCK * IPT;
     constexpr int NIMG = KIND == K_S1_IMG ? 2 * EMAX + 1 : 1;
     __shared__ __align__(16) float4 sp[2][T];
     __shared__ __align__(16) float se[2][T];
     __shared__ __align__(16) uint32_t sid[2][T];
+    __shared__ __align__(16) float4 sres[2][T];
     __shared__ int s_item;
     const int tid = threadIdx.x;
 
@@ -75,11 +76,11 @@ __global__ void __launch_bounds__(BLOCK) k_pair_mixed(MixedArgs a)
             ax[k] = ay[k] = az[k] = 0.0;
         }
 
-        if (J0 < J1) stage_tile<BLOCK, IPT>(a, J0, sp[0], se[0], sid[0]);
+        if (J0 < J1) stage_tile<BLOCK, IPT>(a, J0, sp[0], se[0], sid[0], sres[0]);
         for (int J = J0; J < J1; ++J) {
             const int buf = (J - J0) & 1;
             if (J + 1 < J1) {
-                stage_tile<BLOCK, IPT>(a, J + 1, sp[buf ^ 1], se[buf ^ 1], sid[buf ^ 1]);
+                stage_tile<BLOCK, IPT>(a, J + 1, sp[buf ^ 1], se[buf ^ 1], sid[buf ^ 1], sres[buf ^ 1]);
                 cp_wait<1>();
             } else {
                 cp_wait<0>();
@@ -102,7 +103,8 @@ __global__ void __launch_bounds__(BLOCK) k_pair_mixed(MixedArgs a)
             float off[NIMG];
             if (KIND == K_R3) {
                 const float gz = axis_gap(dOz, mI1.z, mJ1.z);
-                full = gx * gx + gy * gy + gz * gz <= bmax2;
+                const float g2 = gx * gx + gy * gy + gz * gz;
+                full = g2 <= bmax2 || coarse_for_gap(dOx, dOy, dOz, mI1, mJ1, g2);
             } else if (KIND == K_S1_IMG) {
                 // Range of dz over the tile pair, then per image m: entirely
                 // inside the cut (offset m L), entirely outside (offset 1e18,
@@ -111,6 +113,7 @@ __global__ void __launch_bounds__(BLOCK) k_pair_mixed(MixedArgs a)
                 const float lo = dOz - hz, hi = dOz + hz;
                 const float g2xy = gx * gx + gy * gy;
                 bool mixed = false, near = false;
+                float g2min = 3.0e38f;
                 const float cin = a.cutL * (1.0f - 1e-6f), cout = a.cutL * (1.0f + 1e-6f);
 #pragma unroll
                 for (int m = 0; m < NIMG; m++) {
@@ -122,12 +125,14 @@ __global__ void __launch_bounds__(BLOCK) k_pair_mixed(MixedArgs a)
                     off[m] = in ? sh : 1e18f;
                     const float gz = (l <= 0.0f && h >= 0.0f) ? 0.0f : fminf(fabsf(l), fabsf(h));
                     near |= !out && (g2xy + gz * gz <= bmax2);
+                    if (!out) g2min = fminf(g2min, g2xy + gz * gz);
                 }
-                full = mixed || near;
+                full = mixed || near || coarse_for_gap(dOx, dOy, dOz, mI1, mJ1, g2min);
             } else {
                 full = true;
             }
 
+            // i in J's frame, rounded to FP32 for the far path.
             float px[IPT], py[IPT], pz[IPT], fx[IPT], fy[IPT], fz[IPT];
 #pragma unroll
             for (int k = 0; k < IPT; k++) {
@@ -139,6 +144,7 @@ __global__ void __launch_bounds__(BLOCK) k_pair_mixed(MixedArgs a)
             const float4 *spb = sp[buf];
             const float *seb = se[buf];
             const uint32_t *sidb = sid[buf];
+            const float4 *sresb = sres[buf];
 
             if (!full) {
                 if (KIND == K_R3) {
@@ -182,6 +188,14 @@ __global__ void __launch_bounds__(BLOCK) k_pair_mixed(MixedArgs a)
                 }
             } else {
                 // Full path: softening per pair (and per image with the cut test).
+                // i in J's frame as a double-float ph + pl.
+                float phx[IPT], phy[IPT], phz[IPT], plx[IPT], ply[IPT], plz[IPT];
+#pragma unroll
+                for (int k = 0; k < IPT; k++) {
+                    frame_split(xi[k], lx[k], dOx, eOx, phx[k], plx[k]);
+                    frame_split(yi[k], ly[k], dOy, eOy, phy[k], ply[k]);
+                    frame_split(zi[k], lz[k], dOz, eOz, phz[k], plz[k]);
+                }
                 // The self pair gets d = 0 exactly, as in the reference: after
                 // the change of tile frame its FP32 separation is a rounding
                 // residue, which the spline core would turn into a force.
@@ -189,11 +203,14 @@ __global__ void __launch_bounds__(BLOCK) k_pair_mixed(MixedArgs a)
                     const float4 q = spb[jj];
                     const float ej = seb[jj];
                     const uint32_t jid = sidb[jj];
+                    const float4 ql = sresb[jj];
 #pragma unroll
                     for (int k = 0; k < IPT; k++) {
                         const bool self = jid == ii[k];
-                        const float dx = self ? 0.0f : q.x - px[k], dy = self ? 0.0f : q.y - py[k];
-                        float dz = self ? 0.0f : q.z - pz[k];
+                        // double-float separation: ~1e-7 of |d| whatever the tile size
+                        const float dx = self ? 0.0f : (q.x - phx[k]) + (ql.x - plx[k]);
+                        const float dy = self ? 0.0f : (q.y - phy[k]) + (ql.y - ply[k]);
+                        float dz = self ? 0.0f : (q.z - phz[k]) + (ql.z - plz[k]);
                         const float b = ei[k] + ej;
                         const float b2 = b * b;
                         if (KIND == K_R3) {
@@ -214,12 +231,25 @@ __global__ void __launch_bounds__(BLOCK) k_pair_mixed(MixedArgs a)
                             }
                             float sw = 0.0f, swz = 0.0f;
                             for (int m = mlo; m <= mhi; m++) {
-                                const float dzm = dz + (float)m * a.L;
+                                const float sh = (float)m * a.L;
+                                const float dzm = dz + sh;
                                 const float r2 = fmaf(dzm, dzm, rho2);
                                 const float ri = rsqrt_mufu(r2);
                                 float w = ri * ri * ri;
                                 if (r2 < b2) w = spline_inner_f32(r2, b);
-                                if (!a.nearest && !(fabsf(dzm) <= a.cutL)) w = 0.0f;
+                                if (!a.nearest) {
+                                    // |dz + mL| <= (e - 0.4) L (StePS/src/forces.cc:1274), a hard
+                                    // cut: within a hair of it, decide on a TwoSum-exact dz.
+                                    bool in = fabsf(dzm) <= a.cutL;
+                                    if (!self && fabsf(fabsf(dzm) - a.cutL) < a.cut_tol) {
+                                        float e1, e2;
+                                        const float s1 = two_diff(q.z, phz[k], e1);
+                                        const float hh = two_diff(s1, -sh, e2);
+                                        const float tail = e2 + (e1 + (ql.z - plz[k]));
+                                        in = (fabsf(hh) - a.cutL) + copysignf(1.0f, hh) * tail <= 0.0f;
+                                    }
+                                    if (!in) w = 0.0f;
+                                }
                                 sw += w;
                                 swz = fmaf(w, dzm, swz);
                             }
@@ -307,33 +337,41 @@ bool shape_supported_for(const KParams &kp, int threads, int ipt)
 {
     size_t dyn;
     if (kp.topology == STEPS_T3) return t3_kernel(kp, threads, ipt, &dyn) != nullptr;
+    if (kp.topology == STEPS_S1R2 && kp.is_periodic >= 2 && !kp.s1r2_images)
+        return s1tab_kernel(kp, threads, ipt) != nullptr;
     return select_kernel(kp, threads, ipt) != nullptr;
 }
 
 bool mixed_supported(const KParams &kp) { return select_kernel(kp, 128, 2) != nullptr; }
 
-void forces_mixed(const KParams &kp, const Tables &tb, const double *x, int n, int id_min, int ni, double *F,
-                  bool reuse_order)
+void forces_mixed(const KParams &kp, const Tables &tb, const double *x, const double *m64, const double *eps64,
+                  int n, int id_min, int ni, double *F, bool reuse_order)
 {
     Ctx &c = ctx();
     cudaStream_t st = c.stream;
     const int threads = c.shape.threads, ipt = c.shape.ipt;
     const int T = threads * ipt;
     size_t dyn = 0;
-    KernelFn fn = kp.topology == STEPS_T3 ? t3_kernel(kp, threads, ipt, &dyn) : select_kernel(kp, threads, ipt);
+    const bool s1tab = kp.topology == STEPS_S1R2 && kp.is_periodic >= 2 && !kp.s1r2_images;
+    const bool packed = kp.topology == STEPS_R3 && c.shape.variant == 1;
+    KernelFn fn = kp.topology == STEPS_T3 ? t3_kernel(kp, threads, ipt, &dyn)
+                  : s1tab              ? s1tab_kernel(kp, threads, ipt)
+                  : packed             ? r3x2_kernel(threads, ipt)
+                                       : select_kernel(kp, threads, ipt);
     if (!fn) fail(STEPS_E_ARG, "mixed precision: unsupported topology/mode or kernel shape");
 
     unsigned long long *bb = c.bbox.ensure<unsigned long long>(8);
     STEPS_CUDA(cudaEventRecord(c.phase[0], st));
-    build_tiles(c.tj, x, c.m64.as<double>(), c.eps64.as<double>(), 0, n, T, reuse_order, st, bb, PAD_J);
+    build_tiles(c.tj, x, m64, eps64, 0, n, T, reuse_order, st, bb, PAD_J);
     const bool full_i = id_min == 0 && ni == n;
     TileSet &ti = full_i ? c.tj : c.ti;
     if (!full_i)
-        build_tiles(c.ti, x, c.m64.as<double>(), c.eps64.as<double>(), id_min, ni, T, reuse_order, st, bb, PAD_I);
+        build_tiles(c.ti, x, m64, eps64, id_min, ni, T, reuse_order, st, bb, PAD_I);
     STEPS_CUDA(cudaEventRecord(c.phase[1], st));
 
     // Work decomposition: items = i tiles x j chunks, sized so the persistent
     // grid sees several waves with a small last-wave remainder.
+    if (dyn > 0) STEPS_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
     int occ = 0;
     STEPS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, threads, dyn));
     if (occ < 1) occ = 1;
@@ -362,6 +400,8 @@ void forces_mixed(const KParams &kp, const Tables &tb, const double *x, int n, i
     a.jeps = c.tj.eps.as<float>();
     a.jmeta = c.tj.meta.as<float4>();
     a.jidx = c.tj.idx.as<uint32_t>();
+    a.jres = c.tj.resid.as<float4>();
+    a.jsoa = c.tj.soa.as<float>();
     a.njt = njt;
     a.ipack = ti.pack.as<float4>();
     a.ieps = ti.eps.as<float>();
@@ -373,18 +413,24 @@ void forces_mixed(const KParams &kp, const Tables &tb, const double *x, int n, i
     a.tpc = tpc;
     a.nitems = nit * S;
     a.counter = c.counter.ensure<unsigned>(4);
+    a.items = nullptr;
     a.part_stride = (size_t)nit * T * 3;
     a.part = c.partial.ensure<double>((size_t)S * a.part_stride);
     a.L = (float)kp.L;
     a.halfL = (float)kp.halfL;
     a.cutL = (float)kp.cutL;
+    a.cut_tol = (float)(kp.cutL * 1e-5);
     a.emax = kp.emax;
     a.nearest = kp.topology == STEPS_S1R2 && kp.is_periodic < 2;
     a.t3f = nullptr;
     a.ng = 0;
     a.ih = a.u0 = 0.0f;
     a.wcap = 0;
+    a.s1tab = nullptr;
+    a.nrho = a.nz = 0;
+    a.irho = a.iz = a.rho_max = 0.0f;
     if (kp.topology == STEPS_T3) t3_args(a, kp, tb, st);
+    if (s1tab) s1tab_args(a, kp, tb, st);
 
     STEPS_CUDA(cudaMemsetAsync(a.counter, 0, sizeof(unsigned), st));
     int grid = resident < a.nitems ? resident : a.nitems;

@@ -1,0 +1,273 @@
+// Mixed-precision R^3 kernel on packed FP32 pairs (PTX .f32x2 add/sub/mul/fma,
+// sm_100+): the same algorithm, tiling and accuracy as k_pair_mixed<K_R3>
+// (pair_mixed.cu), with the far-field pair arithmetic issued two pairs per
+// instruction.
+//
+// The scalar far-field loop needs 12 FP32 instructions + 1 MUFU + 1/ipt LDS
+// per pair and is issue-bound (one instruction per cycle per SM sub-partition).
+// Packed, one thread holds each i as a broadcast pair {p, p} and meets two j
+// particles at a time: X[jj..jj+1] from the tile's SoA block in shared memory
+// is already the packed operand {q_jj, q_jj+1}. Per two pairs: 3 FADD2 (d),
+// FMUL2 + 2 FFMA2 (r^2), 2 MUFU rsqrt, 3 FMUL2 (m r^-3), 3 FFMA2 (accumulate)
+// -- 14 issue slots, so the FMA pipe rather than issue becomes the limit.
+// Near-field tile pairs (and tile pairs whose FP32 scale is coarse for their
+// gap) run the scalar double-float spline path, reading the same SoA block.
+#include "common.cuh"
+#include "context.cuh"
+#include "mixed.cuh"
+
+namespace steps {
+
+namespace {
+
+using namespace mixed;
+
+typedef unsigned long long f2;  // two FP32 values in a 64-bit register pair; low half = first
+
+__device__ __forceinline__ f2 f2_bcast(float v)
+{
+    f2 r;
+    asm("mov.b64 %0, {%1, %1};" : "=l"(r) : "f"(v));
+    return r;
+}
+__device__ __forceinline__ f2 f2_pack(float lo, float hi)
+{
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void f2_unpack(f2 v, float &lo, float &hi)
+{
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f2 f2_sub(f2 a, f2 b)
+{
+    f2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 f2_mul(f2 a, f2 b)
+{
+    f2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 f2_fma(f2 a, f2 b, f2 c)
+{
+    f2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+
+template <int BLOCK, int IPT>
+__device__ __forceinline__ void stage_soa(const MixedArgs &a, int J, float *sx, float *se, uint32_t *sid, float4 *sres)
+{
+    constexpr int T = BLOCK * IPT;
+    const float4 *src = reinterpret_cast<const float4 *>(a.jsoa + (size_t)J * 4 * T);
+    float4 *dst = reinterpret_cast<float4 *>(sx);
+#pragma unroll
+    for (int k = 0; k < IPT; k++) {  // 4T floats = T float4 chunks
+        const int e = k * BLOCK + threadIdx.x;
+        const size_t q = (size_t)J * T + e;
+        cp_async16(dst + e, src + e);
+        cp_async4(se + e, a.jeps + q);
+        cp_async4(sid + e, a.jidx + q);
+        cp_async16(sres + e, a.jres + q);
+    }
+    cp_commit();
+}
+
+template <int BLOCK, int IPT, bool LIST>
+__global__ void __launch_bounds__(BLOCK) k_pair_r3x2(MixedArgs a)
+{
+    constexpr int T = BLOCK * IPT;
+    __shared__ __align__(16) float sx[2][4 * T];  // X[T], Y[T], Z[T], M[T]
+    __shared__ __align__(16) float se[2][T];
+    __shared__ __align__(16) uint32_t sid[2][T];
+    __shared__ __align__(16) float4 sres[2][T];
+    __shared__ int s_item;
+    const int tid = threadIdx.x;
+
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) s_item = (int)atomicAdd(a.counter, 1u);
+        __syncthreads();
+        const int item = s_item;
+        if (item >= a.nitems) return;
+        int I, J0, J1;
+        size_t base;  // where this item's T partial forces go
+        if (LIST) {
+            const int4 d = __ldg(a.items + item);
+            I = d.x;
+            J0 = d.y;
+            J1 = d.z;
+            base = (size_t)d.w * 3 * T;
+        } else {
+            I = item / a.S;
+            const int chunk = item - I * a.S;
+            J0 = chunk * a.tpc;
+            J1 = min(a.njt, J0 + a.tpc);
+            base = (size_t)chunk * a.part_stride + 3 * (size_t)I * T;
+        }
+
+        const float4 mI0 = __ldg(a.imeta + 2 * I);
+        const float4 mI1 = __ldg(a.imeta + 2 * I + 1);
+        float xi[IPT], yi[IPT], zi[IPT], ei[IPT], lx[IPT], ly[IPT], lz[IPT];
+        uint32_t ii[IPT];
+        double ax[IPT], ay[IPT], az[IPT];
+#pragma unroll
+        for (int k = 0; k < IPT; k++) {
+            const size_t q = (size_t)I * T + k * BLOCK + tid;
+            const float4 p = __ldg(a.ipack + q);
+            xi[k] = p.x;
+            yi[k] = p.y;
+            zi[k] = p.z;
+            ei[k] = __ldg(a.ieps + q);
+            ii[k] = __ldg(a.iidx + q);
+            const float4 l = __ldg(a.ilo + q);
+            lx[k] = l.x;
+            ly[k] = l.y;
+            lz[k] = l.z;
+            ax[k] = ay[k] = az[k] = 0.0;
+        }
+
+        if (J0 < J1) stage_soa<BLOCK, IPT>(a, J0, sx[0], se[0], sid[0], sres[0]);
+        for (int J = J0; J < J1; ++J) {
+            const int buf = (J - J0) & 1;
+            if (J + 1 < J1) {
+                stage_soa<BLOCK, IPT>(a, J + 1, sx[buf ^ 1], se[buf ^ 1], sid[buf ^ 1], sres[buf ^ 1]);
+                cp_wait<1>();
+            } else {
+                cp_wait<0>();
+            }
+            __syncthreads();
+
+            const float4 mJ0 = __ldg(a.jmeta + 2 * J);
+            const float4 mJ1 = __ldg(a.jmeta + 2 * J + 1);
+            float eOx, eOy, eOz;
+            const float dOx = two_diff(mJ0.x, mI0.x, eOx), dOy = two_diff(mJ0.y, mI0.y, eOy),
+                        dOz = two_diff(mJ0.z, mI0.z, eOz);
+            const float bmax = mI0.w + mJ0.w;
+            const float gx = axis_gap(dOx, mI1.x, mJ1.x), gy = axis_gap(dOy, mI1.y, mJ1.y),
+                        gz = axis_gap(dOz, mI1.z, mJ1.z);
+            const float g2 = gx * gx + gy * gy + gz * gz;
+            const bool full = g2 <= bmax * bmax * 1.0001f + 1e-30f || coarse_for_gap(dOx, dOy, dOz, mI1, mJ1, g2);
+            const float *X = sx[buf];
+            const float *Y = X + T;
+            const float *Z = X + 2 * T;
+            const float *Mq = X + 3 * T;
+
+            if (!full) {
+                f2 PX[IPT], PY[IPT], PZ[IPT], AX[IPT], AY[IPT], AZ[IPT];
+#pragma unroll
+                for (int k = 0; k < IPT; k++) {
+                    PX[k] = f2_bcast(((xi[k] - dOx) - eOx) + lx[k]);
+                    PY[k] = f2_bcast(((yi[k] - dOy) - eOy) + ly[k]);
+                    PZ[k] = f2_bcast(((zi[k] - dOz) - eOz) + lz[k]);
+                    AX[k] = AY[k] = AZ[k] = 0ull;  // {+0, +0}
+                }
+#pragma unroll 2
+                for (int jj = 0; jj < T; jj += 4) {
+                    const ulonglong2 qx4 = *reinterpret_cast<const ulonglong2 *>(X + jj);
+                    const ulonglong2 qy4 = *reinterpret_cast<const ulonglong2 *>(Y + jj);
+                    const ulonglong2 qz4 = *reinterpret_cast<const ulonglong2 *>(Z + jj);
+                    const ulonglong2 qm4 = *reinterpret_cast<const ulonglong2 *>(Mq + jj);
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        const f2 qx = h ? qx4.y : qx4.x, qy = h ? qy4.y : qy4.x, qz = h ? qz4.y : qz4.x;
+                        const f2 qm = h ? qm4.y : qm4.x;
+#pragma unroll
+                        for (int k = 0; k < IPT; k++) {
+                            const f2 dx = f2_sub(qx, PX[k]), dy = f2_sub(qy, PY[k]), dz = f2_sub(qz, PZ[k]);
+                            const f2 r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx)));
+                            float r2a, r2b;
+                            f2_unpack(r2, r2a, r2b);
+                            const f2 ri = f2_pack(rsqrt_mufu(r2a), rsqrt_mufu(r2b));
+                            const f2 w = f2_mul(f2_mul(qm, ri), f2_mul(ri, ri));
+                            AX[k] = f2_fma(w, dx, AX[k]);
+                            AY[k] = f2_fma(w, dy, AY[k]);
+                            AZ[k] = f2_fma(w, dz, AZ[k]);
+                        }
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < IPT; k++) {
+                    float l0, l1;
+                    f2_unpack(AX[k], l0, l1);
+                    ax[k] += (double)(l0 + l1);
+                    f2_unpack(AY[k], l0, l1);
+                    ay[k] += (double)(l0 + l1);
+                    f2_unpack(AZ[k], l0, l1);
+                    az[k] += (double)(l0 + l1);
+                }
+            } else {
+                // Near field: scalar double-float path with the spline
+                // (StePS/src/forces.cc:52-87); the self pair gets d = 0.
+                float phx[IPT], phy[IPT], phz[IPT], plx[IPT], ply[IPT], plz[IPT], fx[IPT], fy[IPT], fz[IPT];
+#pragma unroll
+                for (int k = 0; k < IPT; k++) {
+                    frame_split(xi[k], lx[k], dOx, eOx, phx[k], plx[k]);
+                    frame_split(yi[k], ly[k], dOy, eOy, phy[k], ply[k]);
+                    frame_split(zi[k], lz[k], dOz, eOz, phz[k], plz[k]);
+                    fx[k] = fy[k] = fz[k] = 0.0f;
+                }
+                const float *seb = se[buf];
+                const uint32_t *sidb = sid[buf];
+                const float4 *sresb = sres[buf];
+                for (int jj = 0; jj < T; ++jj) {
+                    const float qx = X[jj], qy = Y[jj], qz = Z[jj], qm = Mq[jj];
+                    const float ej = seb[jj];
+                    const uint32_t jid = sidb[jj];
+                    const float4 ql = sresb[jj];
+#pragma unroll
+                    for (int k = 0; k < IPT; k++) {
+                        const bool self = jid == ii[k];
+                        const float dx = self ? 0.0f : (qx - phx[k]) + (ql.x - plx[k]);
+                        const float dy = self ? 0.0f : (qy - phy[k]) + (ql.y - ply[k]);
+                        const float dz = self ? 0.0f : (qz - phz[k]) + (ql.z - plz[k]);
+                        const float b = ei[k] + ej;
+                        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                        const float ri = rsqrt_mufu(r2);
+                        float w = ri * ri * ri;
+                        if (r2 < b * b) w = spline_inner_f32(r2, b);
+                        w *= qm;
+                        fx[k] = fmaf(w, dx, fx[k]);
+                        fy[k] = fmaf(w, dy, fy[k]);
+                        fz[k] = fmaf(w, dz, fz[k]);
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < IPT; k++) {
+                    ax[k] += (double)fx[k];
+                    ay[k] += (double)fy[k];
+                    az[k] += (double)fz[k];
+                }
+            }
+            __syncthreads();
+        }
+
+        double *o = a.part + base;
+#pragma unroll
+        for (int k = 0; k < IPT; k++) {
+            const size_t e = k * BLOCK + tid;
+            o[3 * e] = ax[k];
+            o[3 * e + 1] = ay[k];
+            o[3 * e + 2] = az[k];
+        }
+    }
+}
+
+}  // namespace
+
+KernelFn r3x2_kernel(int threads, int ipt, bool list)
+{
+#define STEPS_SHAPE(B, P) \
+    if (threads == B && ipt == P) return list ? k_pair_r3x2<B, P, true> : k_pair_r3x2<B, P, false>;
+    STEPS_SHAPE(64, 1) STEPS_SHAPE(64, 2) STEPS_SHAPE(64, 4)
+    STEPS_SHAPE(128, 1) STEPS_SHAPE(128, 2) STEPS_SHAPE(128, 4)
+    STEPS_SHAPE(256, 1) STEPS_SHAPE(256, 2)
+#undef STEPS_SHAPE
+    return nullptr;
+}
+
+}  // namespace steps

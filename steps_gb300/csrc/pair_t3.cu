@@ -55,6 +55,7 @@ __global__ void __launch_bounds__(BLOCK) k_pair_t3(MixedArgs a)
     __shared__ __align__(16) float4 sp[2][T];
     __shared__ __align__(16) float se[2][T];
     __shared__ __align__(16) uint32_t sid[2][T];
+    __shared__ __align__(16) float4 sres[2][T];
     __shared__ int s_item;
     extern __shared__ float4 win[];
     const int tid = threadIdx.x;
@@ -92,7 +93,7 @@ __global__ void __launch_bounds__(BLOCK) k_pair_t3(MixedArgs a)
             ax[k] = ay[k] = az[k] = 0.0;
         }
 
-        if (J0 < J1) stage_tile<BLOCK, IPT>(a, J0, sp[0], se[0], sid[0]);
+        if (J0 < J1) stage_tile<BLOCK, IPT>(a, J0, sp[0], se[0], sid[0], sres[0]);
         for (int J = J0; J < J1; ++J) {
             const int buf = (J - J0) & 1;
             const float4 mJ0 = __ldg(a.jmeta + 2 * J);
@@ -122,12 +123,13 @@ __global__ void __launch_bounds__(BLOCK) k_pair_t3(MixedArgs a)
             // Pairs closer than some beta = eps_i + eps_j need the spline; a
             // wrapped axis makes the box gap meaningless, so take the full path.
             const float bmax = mI0.w + mJ0.w;
-            const bool full = g2 <= bmax * bmax * 1.0001f + 1e-30f || wrap[0] || wrap[1] || wrap[2];
+            const bool full = g2 <= bmax * bmax * 1.0001f + 1e-30f || wrap[0] || wrap[1] || wrap[2] ||
+                              coarse_for_gap(dO[0], dO[1], dO[2], mI1, mJ1, g2);
             const int ncell = ORDER != 0 ? wn[0] * wn[1] * wn[2] : 0;
             const bool use_win = ORDER != 0 && ncell <= a.wcap;
 
             if (J + 1 < J1) {
-                stage_tile<BLOCK, IPT>(a, J + 1, sp[buf ^ 1], se[buf ^ 1], sid[buf ^ 1]);
+                stage_tile<BLOCK, IPT>(a, J + 1, sp[buf ^ 1], se[buf ^ 1], sid[buf ^ 1], sres[buf ^ 1]);
                 cp_wait<1>();
             } else {
                 cp_wait<0>();
@@ -143,17 +145,22 @@ __global__ void __launch_bounds__(BLOCK) k_pair_t3(MixedArgs a)
             }
             __syncthreads();
 
+            float phx[IPT], phy[IPT], phz[IPT], plx[IPT], ply[IPT], plz[IPT];
             float px[IPT], py[IPT], pz[IPT], fx[IPT], fy[IPT], fz[IPT];
 #pragma unroll
             for (int k = 0; k < IPT; k++) {
-                px[k] = ((xi[k] - dO[0]) - eO[0]) + lx[k];
-                py[k] = ((yi[k] - dO[1]) - eO[1]) + ly[k];
-                pz[k] = ((zi[k] - dO[2]) - eO[2]) + lz[k];
+                frame_split(xi[k], lx[k], dO[0], eO[0], phx[k], plx[k]);
+                frame_split(yi[k], ly[k], dO[1], eO[1], phy[k], ply[k]);
+                frame_split(zi[k], lz[k], dO[2], eO[2], phz[k], plz[k]);
+                px[k] = phx[k] + plx[k];
+                py[k] = phy[k] + ply[k];
+                pz[k] = phz[k] + plz[k];
                 fx[k] = fy[k] = fz[k] = 0.0f;
             }
             const float4 *spb = sp[buf];
             const float *seb = se[buf];
             const uint32_t *sidb = sid[buf];
+            const float4 *sresb = sres[buf];
             const int sy = ORDER != 0 ? wn[2] : 0, sx = ORDER != 0 ? wn[1] * wn[2] : 0;
 
 #pragma unroll 2
@@ -164,9 +171,17 @@ __global__ void __launch_bounds__(BLOCK) k_pair_t3(MixedArgs a)
 #pragma unroll
                 for (int k = 0; k < IPT; k++) {
                     const bool self = full && jid == ii[k];
-                    const float dx = self ? 0.0f : q.x - px[k];
-                    const float dy = self ? 0.0f : q.y - py[k];
-                    const float dz = self ? 0.0f : q.z - pz[k];
+                    float dx, dy, dz;
+                    if (full) {  // double-float separation
+                        const float4 ql = sresb[jj];
+                        dx = self ? 0.0f : (q.x - phx[k]) + (ql.x - plx[k]);
+                        dy = self ? 0.0f : (q.y - phy[k]) + (ql.y - ply[k]);
+                        dz = self ? 0.0f : (q.z - phz[k]) + (ql.z - plz[k]);
+                    } else {
+                        dx = q.x - px[k];
+                        dy = q.y - py[k];
+                        dz = q.z - pz[k];
+                    }
                     float nx = dx, ny = dy, nz = dz;
                     if (wrap[0]) nx = fabsf(nx) > halfL ? nx - copysignf(L, nx) : nx;
                     if (wrap[1]) ny = fabsf(ny) > halfL ? ny - copysignf(L, ny) : ny;
@@ -193,7 +208,7 @@ __global__ void __launch_bounds__(BLOCK) k_pair_t3(MixedArgs a)
                             by = (int)fyl - OFF;
                             bz = (int)fzl - OFF;
                             const float4 *base = win + (bx * sx + by * sy + bz);
-#pragma unroll
+#pragma unroll(ORDER == 4 ? 1 : NT)
                             for (int aa = 0; aa < NT; aa++)
 #pragma unroll
                                 for (int bb = 0; bb < NT; bb++) {
@@ -259,6 +274,213 @@ __global__ void __launch_bounds__(BLOCK) k_pair_t3(MixedArgs a)
     }
 }
 
+// (rho, z) table interpolation in FP32 from the float2 copy of the S1xR2
+// table: NGP / CIC / TSC exactly as StePS/src/ewald_space.cc:803-1000
+// (rho clamped to [0, rho_max], z index periodic).
+template <int ORDER>
+__device__ __forceinline__ void s1r2_interp_f32(const float2 *__restrict__ T, int nrho, int nz, float irho,
+                                                float rho_max, float iz, float halfL, float rho, float z, float &Dr,
+                                                float &Dz)
+{
+    const float rr = fminf(fmaxf(rho, 0.0f), rho_max);
+    const float ur = rr * irho;
+    const float uz = (z + halfL) * iz - 0.5f;
+    Dr = 0.0f;
+    Dz = 0.0f;
+    if (ORDER == 0) {
+        int ir = (int)floorf(ur + 0.5f);
+        ir = ir < 0 ? 0 : (ir > nrho - 1 ? nrho - 1 : ir);
+        const int izc = pmod((int)floorf(uz + 0.5f), nz);
+        const float2 v = __ldg(T + (size_t)ir * nz + izc);
+        Dr = v.x;
+        Dz = v.y;
+    } else if (ORDER == 2) {
+        int ir0 = (int)floorf(ur);
+        float fr = ur - (float)ir0;
+        if (ir0 < 0) { ir0 = 0; fr = 0.0f; }
+        if (ir0 > nrho - 2) { ir0 = nrho - 2 > 0 ? nrho - 2 : 0; fr = 1.0f; }
+        const int iz0f = (int)floorf(uz);
+        const float fz = uz - (float)iz0f;
+        const int iz0 = pmod(iz0f, nz), iz1 = pmod(iz0 + 1, nz);
+        const float2 a00 = __ldg(T + (size_t)ir0 * nz + iz0), a10 = __ldg(T + (size_t)(ir0 + 1) * nz + iz0);
+        const float2 a01 = __ldg(T + (size_t)ir0 * nz + iz1), a11 = __ldg(T + (size_t)(ir0 + 1) * nz + iz1);
+        const float w00 = (1.0f - fr) * (1.0f - fz), w10 = fr * (1.0f - fz), w01 = (1.0f - fr) * fz, w11 = fr * fz;
+        Dr = w00 * a00.x + w10 * a10.x + w01 * a01.x + w11 * a11.x;
+        Dz = w00 * a00.y + w10 * a10.y + w01 * a01.y + w11 * a11.y;
+    } else {
+        const int jr = (int)floorf(ur + 0.5f), jz = (int)floorf(uz + 0.5f);
+        const float sr = ur - (float)jr, sz = uz - (float)jz;
+        const float wr[3] = {0.5f * (0.5f - sr) * (0.5f - sr), 0.75f - sr * sr, 0.5f * (0.5f + sr) * (0.5f + sr)};
+        const float wz[3] = {0.5f * (0.5f - sz) * (0.5f - sz), 0.75f - sz * sz, 0.5f * (0.5f + sz) * (0.5f + sz)};
+        int ir[3] = {jr - 1, jr, jr + 1};
+        if (ir[0] < 0) ir[0] = 0;
+        if (ir[1] < 0) ir[1] = 0;
+        if (ir[1] > nrho - 1) ir[1] = nrho - 1;
+        if (ir[2] > nrho - 1) ir[2] = nrho - 1;
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const int izc = pmod(jz - 1 + c, nz);
+#pragma unroll
+            for (int r = 0; r < 3; r++) {
+                const float2 v = __ldg(T + (size_t)ir[r] * nz + izc);
+                const float w = wr[r] * wz[c];
+                Dr = fmaf(w, v.x, Dr);
+                Dz = fmaf(w, v.y, Dz);
+            }
+        }
+    }
+}
+
+// S1xR2 with the (rho, z) correction table (StePS/src/forces.cc:1307-1350):
+// nearest image along z, softened Newton, minus m_j D(rho, dz).
+template <int BLOCK, int IPT, int ORDER>
+__global__ void __launch_bounds__(BLOCK) k_pair_s1tab(MixedArgs a)
+{
+    constexpr int T = BLOCK * IPT;
+    __shared__ __align__(16) float4 sp[2][T];
+    __shared__ __align__(16) float se[2][T];
+    __shared__ __align__(16) uint32_t sid[2][T];
+    __shared__ __align__(16) float4 sres[2][T];
+    __shared__ int s_item;
+    const int tid = threadIdx.x;
+    const float L = a.L, halfL = a.halfL;
+    const float2 *tab = a.s1tab;
+    const float irho = a.irho, iz = a.iz, rho_max = a.rho_max;
+
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) s_item = (int)atomicAdd(a.counter, 1u);
+        __syncthreads();
+        const int item = s_item;
+        if (item >= a.nitems) return;
+        const int I = item / a.S;
+        const int chunk = item - I * a.S;
+        const int J0 = chunk * a.tpc;
+        const int J1 = min(a.njt, J0 + a.tpc);
+
+        const float4 mI0 = __ldg(a.imeta + 2 * I);
+        const float4 mI1 = __ldg(a.imeta + 2 * I + 1);
+        float xi[IPT], yi[IPT], zi[IPT], ei[IPT], lx[IPT], ly[IPT], lz[IPT];
+        uint32_t ii[IPT];
+        double ax[IPT], ay[IPT], az[IPT];
+#pragma unroll
+        for (int k = 0; k < IPT; k++) {
+            size_t q = (size_t)I * T + k * BLOCK + tid;
+            float4 p = __ldg(a.ipack + q);
+            xi[k] = p.x;
+            yi[k] = p.y;
+            zi[k] = p.z;
+            ei[k] = __ldg(a.ieps + q);
+            ii[k] = __ldg(a.iidx + q);
+            const float4 l = __ldg(a.ilo + q);
+            lx[k] = l.x;
+            ly[k] = l.y;
+            lz[k] = l.z;
+            ax[k] = ay[k] = az[k] = 0.0;
+        }
+
+        if (J0 < J1) stage_tile<BLOCK, IPT>(a, J0, sp[0], se[0], sid[0], sres[0]);
+        for (int J = J0; J < J1; ++J) {
+            const int buf = (J - J0) & 1;
+            if (J + 1 < J1) {
+                stage_tile<BLOCK, IPT>(a, J + 1, sp[buf ^ 1], se[buf ^ 1], sid[buf ^ 1], sres[buf ^ 1]);
+                cp_wait<1>();
+            } else {
+                cp_wait<0>();
+            }
+            __syncthreads();
+            const float4 mJ0 = __ldg(a.jmeta + 2 * J);
+            const float4 mJ1 = __ldg(a.jmeta + 2 * J + 1);
+            float eOx, eOy, eOz;
+            const float dOx = two_diff(mJ0.x, mI0.x, eOx), dOy = two_diff(mJ0.y, mI0.y, eOy);
+            float dOz = two_diff(mJ0.z, mI0.z, eOz);
+            dOz -= L * rintf(dOz / L);  // nearest image of J's centre along z
+            const float hz = mI1.z + mJ1.z;
+            const bool wrapz = fabsf(dOz) + hz > halfL;
+            const float gx = axis_gap(dOx, mI1.x, mJ1.x), gy = axis_gap(dOy, mI1.y, mJ1.y);
+            const float gz = axis_gap(dOz, mI1.z, mJ1.z);
+            const float bmax = mI0.w + mJ0.w;
+            const float g2 = gx * gx + gy * gy + gz * gz;
+            const bool full = wrapz || g2 <= bmax * bmax * 1.0001f + 1e-30f || coarse_for_gap(dOx, dOy, dOz, mI1, mJ1, g2);
+
+            float phx[IPT], phy[IPT], phz[IPT], plx[IPT], ply[IPT], plz[IPT];
+            float fx[IPT], fy[IPT], fz[IPT];
+#pragma unroll
+            for (int k = 0; k < IPT; k++) {
+                frame_split(xi[k], lx[k], dOx, eOx, phx[k], plx[k]);
+                frame_split(yi[k], ly[k], dOy, eOy, phy[k], ply[k]);
+                frame_split(zi[k], lz[k], dOz, eOz, phz[k], plz[k]);
+                fx[k] = fy[k] = fz[k] = 0.0f;
+            }
+            const float4 *spb = sp[buf];
+            const float *seb = se[buf];
+            const uint32_t *sidb = sid[buf];
+            const float4 *sresb = sres[buf];
+            for (int jj = 0; jj < T; ++jj) {
+                const float4 q = spb[jj];
+                const float ej = seb[jj];
+                const uint32_t jid = sidb[jj];
+#pragma unroll
+                for (int k = 0; k < IPT; k++) {
+                    const bool self = full && jid == ii[k];
+                    const float4 ql = sresb[jj];
+                    const float dx = self ? 0.0f : (q.x - phx[k]) + (ql.x - plx[k]);
+                    const float dy = self ? 0.0f : (q.y - phy[k]) + (ql.y - ply[k]);
+                    float dz = self ? 0.0f : (q.z - phz[k]) + (ql.z - plz[k]);
+                    if (wrapz) dz = fabsf(dz) > halfL ? dz - copysignf(L, dz) : dz;
+                    const float rho2 = fmaf(dx, dx, dy * dy);
+                    const float r2 = fmaf(dz, dz, rho2);
+                    const float ri = rsqrt_mufu(r2);
+                    float w = ri * ri * ri;
+                    if (full) {
+                        const float b = ei[k] + ej;
+                        if (r2 < b * b) w = spline_inner_f32(r2, b);
+                    }
+                    const float rho = sqrt_mufu(rho2);
+                    float Dr, Dz;
+                    s1r2_interp_f32<ORDER>(tab, a.nrho, a.nz, irho, rho_max, iz, halfL, rho, dz, Dr, Dz);
+                    const float er = rho > 0.0f ? Dr * rcp_mufu(rho) : 0.0f;
+                    fx[k] = fmaf(q.w, fmaf(w, dx, -er * dx), fx[k]);
+                    fy[k] = fmaf(q.w, fmaf(w, dy, -er * dy), fy[k]);
+                    fz[k] = fmaf(q.w, fmaf(w, dz, -Dz), fz[k]);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < IPT; k++) {
+                ax[k] += (double)fx[k];
+                ay[k] += (double)fy[k];
+                az[k] += (double)fz[k];
+            }
+            __syncthreads();
+        }
+
+        double *o = a.part + (size_t)chunk * a.part_stride;
+#pragma unroll
+        for (int k = 0; k < IPT; k++) {
+            size_t q = (size_t)I * T + k * BLOCK + tid;
+            o[3 * q] = ax[k];
+            o[3 * q + 1] = ay[k];
+            o[3 * q + 2] = az[k];
+        }
+    }
+}
+
+__global__ void k_table2_f32(const double *__restrict__ t, size_t ncell, float2 *__restrict__ out)
+{
+    size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < ncell) out[c] = make_float2((float)t[2 * c], (float)t[2 * c + 1]);
+}
+
+template <int ORDER>
+KernelFn pick_s1tab(int threads, int ipt)
+{
+#define STEPS_SHAPE(B, P) \
+    if (threads == B && ipt == P) return k_pair_s1tab<B, P, ORDER>;
+    STEPS_SHAPE(64, 1) STEPS_SHAPE(64, 2) STEPS_SHAPE(128, 1) STEPS_SHAPE(128, 2) STEPS_SHAPE(256, 1)
+#undef STEPS_SHAPE
+    return nullptr;
+}
+
 __global__ void k_table_f32(const double *__restrict__ t, size_t ncell, float4 *__restrict__ out)
 {
     size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -314,6 +536,32 @@ void t3_args(MixedArgs &a, const KParams &kp, const Tables &tb, cudaStream_t st)
         a.ih = (float)((double)tb.t3_ng / kp.L);
         a.u0 = (float)((double)tb.t3_ng * 0.5 - 0.5);
     }
+}
+
+KernelFn s1tab_kernel(const KParams &kp, int threads, int ipt)
+{
+    if (kp.order == 0) return pick_s1tab<0>(threads, ipt);
+    if (kp.order == 2) return pick_s1tab<2>(threads, ipt);
+    return pick_s1tab<4>(threads, ipt);
+}
+
+void s1tab_args(MixedArgs &a, const KParams &kp, const Tables &tb, cudaStream_t st)
+{
+    Ctx &c = ctx();
+    size_t ncell = (size_t)tb.nrho * tb.nz;
+    if (c.s1f_version != c.s1r2_version || !c.s1f.p) {
+        float2 *o = c.s1f.ensure<float2>(ncell);
+        k_table2_f32<<<(unsigned)((ncell + 255) / 256), 256, 0, st>>>(tb.s1r2, ncell, o);
+        note_launch("k_table2_f32");
+        c.s1f_version = c.s1r2_version;
+    }
+    a.s1tab = c.s1f.as<float2>();
+    a.nrho = tb.nrho;
+    a.nz = tb.nz;
+    const double drho = tb.rho_max / (double)(tb.nrho - 1 > 1 ? tb.nrho - 1 : 1);
+    a.irho = (float)(1.0 / drho);
+    a.iz = (float)((double)tb.nz / kp.L);
+    a.rho_max = (float)tb.rho_max;
 }
 
 }  // namespace steps

@@ -190,6 +190,16 @@ steps_params base_params(int topology)
 
 }  // namespace
 
+/* Overrides the precision chosen at the first call (STEPS_GB300_PRECISION):
+ * STEPS_FP64 or STEPS_MIXED. */
+extern "C" void steps_gb300_legacy_precision(int precision)
+{
+    if (precision == STEPS_FP64 || precision == STEPS_MIXED) {
+        ensure_context();
+        S.precision = precision;
+    }
+}
+
 /* forces.cc:43-50 */
 void recalculate_softening()
 {

@@ -56,6 +56,20 @@ def test_s1r2_other_image_counts(engine, port, isp):
     assert err_stats(engine.forces(ps.x, p, S.MIXED, 0, 511), Fo)["p99"] < MIXED_P99
 
 
+def test_s1r2_images_mixed_large(engine):
+    """The S1xR2 workload's geometry at N = 2^18: at this density some pairs
+    sit within FP32 rounding of the image cut |dz + mL| = 2.6 L; mixed must
+    still agree with FP64 (full-range mixed against an FP64 i subset)."""
+    ps = W.s1r2_cylindrical(1 << 18, 200.0, 600.0, seed=12)
+    engine.set_particles(ps.m, ps.eps)
+    p = S.params(S.S1R2, is_periodic=2, L=200.0, rsim=600.0, s1r2_images=1)
+    Fm = engine.forces(ps.x, p, S.MIXED)
+    lo, hi = 100000, 100767
+    F64 = engine.forces(ps.x, p, S.FP64, lo, hi)
+    st = err_stats(Fm[lo:hi + 1], F64)
+    assert st["p99"] < MIXED_P99, st
+
+
 @pytest.mark.parametrize("order", [0, 2, 4])
 def test_s1r2_table_fp64(engine, order):
     g = golden(f"s1r2_table_o{order}")

@@ -116,6 +116,34 @@ def test_shapes_agree(engine, port):
     engine.set_tuning(128, 2, 0)
 
 
+def test_packed_fp32x2_variant(engine, port):
+    """The packed FP32x2 pair loop agrees with the reference like the scalar one."""
+    g = golden("r3_n2048")
+    engine.set_particles(g["m"], g["eps"])
+    try:
+        engine.set_variant(1)
+        for threads, ipt in ((64, 1), (64, 2), (64, 4), (128, 1), (128, 2), (128, 4), (256, 1), (256, 2)):
+            engine.set_tuning(threads, ipt, 0)
+            st = err_stats(engine.forces(g["x"], S.params(S.R3), S.MIXED), g["F"])
+            assert st["p99"] < MIXED_P99, (threads, ipt, st)
+        engine.set_tuning(128, 2, 0)
+        lo, hi = (int(v) for v in g["sub"])
+        assert err_stats(engine.forces(g["x"], S.params(S.R3), S.MIXED, lo, hi), g["F_sub"])["p99"] < MIXED_P99
+        for n in (3, 129, 1000):
+            ps = W.r3_compactified(n, 300.0, seed=100 + n, displace=True)
+            engine.set_particles(ps.m, ps.eps)
+            Fo = port.forces(port.system(0, ps.m, ps.eps, port_params(O)), ps.x)
+            assert err_stats(engine.forces(ps.x, S.params(S.R3), S.MIXED), Fo)["p99"] < MIXED_P99
+        ps = W.r3_compactified(60000, 1000.0, seed=9, displace=True)
+        engine.set_particles(ps.m, ps.eps)
+        F64 = engine.forces(ps.x, S.params(S.R3), S.FP64, 0, 4095)
+        st = err_stats(engine.forces(ps.x, S.params(S.R3), S.MIXED)[:4096], F64)
+        assert st["p99"] < MIXED_P99, st
+    finally:
+        engine.set_variant(0)
+        engine.set_tuning(128, 2, 0)
+
+
 def test_full_size_subset(engine, port):
     """The cfg1 workload at its full size (N = 2^20): mixed against the FP64
     kernel on an i subset, and the FP64 kernel against the oracle on a
