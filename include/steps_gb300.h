@@ -224,6 +224,25 @@ int steps_gpu_measure_peaks(double *fp32_flops, double *fp64_flops);
 /* Blocks until the library stream is idle; returns a pending kernel error. */
 int steps_gpu_synchronize(void);
 
+/* ---- allocation-free entry point ----------------------------------------- */
+
+/* No counterpart in the reference. Plain FP64 R^3 forces for callers that
+ * cannot allocate device memory: applications that give all device memory to
+ * their own pool allocator, and loops that must not pay the implicit device
+ * synchronisation of cudaMalloc/cudaFree. The caller owns every buffer, all
+ * in device memory of the current device: x[3n] (AoS), m[n], eps[n] and
+ * F[3*(id_max-id_min+1)] (overwritten). Calls no cudaMalloc, cudaFree or
+ * allocating library routine and needs no steps_gpu_init. Asynchronous on
+ * `stream` (a cudaStream_t; NULL = legacy default stream).
+ * Working memory is one static 32 MiB device array per GPU that loads the
+ * library, held until exit: the i range is limited to 1,398,101 particles
+ * (larger ranges return STEPS_E_ARG). The array's device address is looked
+ * up by the first call on each device -- make that call before any stream
+ * capture. All calls share the array (it keeps the last call's contents):
+ * calls that overlap on the GPU race, so the caller serialises them. */
+int steps_gpu_forces_fp64_noalloc(const steps_params *p, const double *x, const double *m, const double *eps, int n,
+                                  double *F, int id_min, int id_max, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
