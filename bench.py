@@ -59,6 +59,7 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=1024, help="i particles in the CPU baseline sample")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--variant", type=int, default=-1, help="R^3 pair loop without autotuning: 0 fp32, 1 fp32x2")
     return ap.parse_args()
 
 
@@ -226,7 +227,9 @@ def run_ours(args, ws, rank, local, dist):
         eng.build_table_t3(*table)
     eng.upload_positions(ps.x)
     f32_peak, f64_peak = eng.measure_peaks()
-    shape = None if args.no_autotune else eng.autotune(p)
+    if args.variant >= 0:
+        eng.set_variant(args.variant)
+    shape = None if (args.no_autotune or args.variant >= 0) else eng.autotune(p)
 
     for _ in range(args.warmup):
         eng.forces_resident(p, S.MIXED)

@@ -191,6 +191,12 @@ int steps_gpu_set_tuning(int threads, int ipt, int jsplit);
  * rounding; the autotuner picks between them. */
 int steps_gpu_set_kernel_variant(int variant);
 
+/* Mixed precision: tile pairs whose coordinate scale (centre distance plus
+ * half extents) exceeds `ratio` times their box gap run the double-float
+ * near-field path instead of the FP32 far-field loop. Lower = more accurate
+ * and slower. Range [1, 1e6]. */
+int steps_gpu_set_precision_guard(double ratio);
+
 /* Times every supported mixed-precision shape (and, for R^3, both pair-loop
  * variants) on the resident particles for the given topology and keeps the
  * fastest; writes threads, ipt, variant to out[3]. */

@@ -210,6 +210,10 @@ class Engine:
         self._check(self.lib.steps_gpu_autotune(C.byref(p), int(id_min), int(id_max), out))
         return int(out[0]), int(out[1]), int(out[2])
 
+    def set_guard(self, ratio: float):
+        self.lib.steps_gpu_set_precision_guard.argtypes = [C.c_double]
+        self._check(self.lib.steps_gpu_set_precision_guard(float(ratio)))
+
     def set_variant(self, variant: int):
         self._check(self.lib.steps_gpu_set_kernel_variant(int(variant)))
 

@@ -448,6 +448,14 @@ int steps_gpu_autotune(const steps_params *p, int id_min, int id_max, int *out)
     });
 }
 
+int steps_gpu_set_precision_guard(double ratio)
+{
+    return guarded([&] {
+        if (!(ratio >= 1.0 && ratio <= 1e6)) fail(STEPS_E_ARG, "precision guard ratio must be in [1, 1e6]");
+        g_ctx.shape.guard = (float)ratio;
+    });
+}
+
 int steps_gpu_set_kernel_variant(int variant)
 {
     return guarded([&] {

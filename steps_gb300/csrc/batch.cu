@@ -202,6 +202,7 @@ void batch_forces(Batch &b)
     a.items = b.items.as<int4>();
     a.counter = b.counter.as<unsigned>();
     a.part = b.part.as<double>();
+    a.guard2 = c.shape.guard * c.shape.guard;
     mixed::KernelFn fn = r3x2_kernel(b.threads, b.ipt, true);
     STEPS_CUDA(cudaMemsetAsync(a.counter, 0, sizeof(unsigned), st));
     fn<<<b.grid, b.threads, 0, st>>>(a);

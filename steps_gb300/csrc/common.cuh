@@ -86,6 +86,7 @@ struct Shape {
     int ipt = 2;
     int jsplit = 0;
     int variant = 0;  // R^3: 0 scalar FP32 pair loop, 1 packed FP32x2 pair loop
+    float guard = 30.0f;  // tile-pair scale / gap above which the double-float path runs
 };
 
 // ------------------------------------------------------------- utilities --

@@ -31,6 +31,7 @@ struct MixedArgs {
     size_t part_stride; // nit*T*3
     float L, halfL, cutL;
     float cut_tol;      // |dz + mL| this close to cutL is re-decided on an exact dz
+    float guard2;       // square of the precision guard ratio (coarse_for_gap)
     int emax;
     int nearest;        // S1R2 IS_PERIODIC == 1: nearest image along z only
     // T^3 Ewald table (FP32 copy, one float4 per cell) and its geometry
@@ -84,14 +85,16 @@ __device__ __forceinline__ float two_diff(float a, float b, float &e)
     return s;
 }
 
-// The FP32 tile offsets carry ~6e-8 of the tile-pair scale |d_O| + h_I + h_J;
-// where that scale exceeds 30x the box gap, a pair can be close enough for
-// this to matter, and the block takes the double-float (full) path.
-__device__ __forceinline__ bool coarse_for_gap(float dOx, float dOy, float dOz, float4 hI, float4 hJ, float g2)
+// The FP32 tile offsets carry ~6e-8 of the tile-pair scale |d_O| + h_I + h_J,
+// so a pair at distance r gets a relative error ~6e-8 * scale / r. Where the
+// scale exceeds `guard` times the box gap (guard2 = guard^2), the block takes
+// the double-float (full) path instead.
+__device__ __forceinline__ bool coarse_for_gap(float dOx, float dOy, float dOz, float4 hI, float4 hJ, float g2,
+                                               float guard2)
 {
     const float s = sqrtf(dOx * dOx + dOy * dOy + dOz * dOz) + sqrtf(hI.x * hI.x + hI.y * hI.y + hI.z * hI.z) +
                     sqrtf(hJ.x * hJ.x + hJ.y * hJ.y + hJ.z * hJ.z);
-    return s * s > 900.0f * g2;
+    return s * s > guard2 * g2;
 }
 
 // i particle k in J's frame as an unevaluated sum ph + pl: ph = fl(x_hi - dO),

@@ -104,7 +104,7 @@ __global__ void __launch_bounds__(BLOCK, KIND == K_R3 && IPT == 1 ? 1024 / BLOCK
             if (KIND == K_R3) {
                 const float gz = axis_gap(dOz, mI1.z, mJ1.z);
                 const float g2 = gx * gx + gy * gy + gz * gz;
-                full = g2 <= bmax2 || coarse_for_gap(dOx, dOy, dOz, mI1, mJ1, g2);
+                full = g2 <= bmax2 || coarse_for_gap(dOx, dOy, dOz, mI1, mJ1, g2, a.guard2);
             } else if (KIND == K_S1_IMG) {
                 // Range of dz over the tile pair, then per image m: entirely
                 // inside the cut (offset m L), entirely outside (offset 1e18,
@@ -127,7 +127,7 @@ __global__ void __launch_bounds__(BLOCK, KIND == K_R3 && IPT == 1 ? 1024 / BLOCK
                     near |= !out && (g2xy + gz * gz <= bmax2);
                     if (!out) g2min = fminf(g2min, g2xy + gz * gz);
                 }
-                full = mixed || near || coarse_for_gap(dOx, dOy, dOz, mI1, mJ1, g2min);
+                full = mixed || near || coarse_for_gap(dOx, dOy, dOz, mI1, mJ1, g2min, a.guard2);
             } else {
                 full = true;
             }
@@ -420,6 +420,7 @@ void forces_mixed(const KParams &kp, const Tables &tb, const double *x, const do
     a.halfL = (float)kp.halfL;
     a.cutL = (float)kp.cutL;
     a.cut_tol = (float)(kp.cutL * 1e-5);
+    a.guard2 = c.shape.guard * c.shape.guard;
     a.emax = kp.emax;
     a.nearest = kp.topology == STEPS_S1R2 && kp.is_periodic < 2;
     a.t3f = nullptr;

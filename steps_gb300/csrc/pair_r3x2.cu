@@ -151,7 +151,7 @@ __global__ void __launch_bounds__(BLOCK) k_pair_r3x2(MixedArgs a)
             const float gx = axis_gap(dOx, mI1.x, mJ1.x), gy = axis_gap(dOy, mI1.y, mJ1.y),
                         gz = axis_gap(dOz, mI1.z, mJ1.z);
             const float g2 = gx * gx + gy * gy + gz * gz;
-            const bool full = g2 <= bmax * bmax * 1.0001f + 1e-30f || coarse_for_gap(dOx, dOy, dOz, mI1, mJ1, g2);
+            const bool full = g2 <= bmax * bmax * 1.0001f + 1e-30f || coarse_for_gap(dOx, dOy, dOz, mI1, mJ1, g2, a.guard2);
             const float *X = sx[buf];
             const float *Y = X + T;
             const float *Z = X + 2 * T;

@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(BLOCK) k_pair_t3(MixedArgs a)
             // wrapped axis makes the box gap meaningless, so take the full path.
             const float bmax = mI0.w + mJ0.w;
             const bool full = g2 <= bmax * bmax * 1.0001f + 1e-30f || wrap[0] || wrap[1] || wrap[2] ||
-                              coarse_for_gap(dO[0], dO[1], dO[2], mI1, mJ1, g2);
+                              coarse_for_gap(dO[0], dO[1], dO[2], mI1, mJ1, g2, a.guard2);
             const int ncell = ORDER != 0 ? wn[0] * wn[1] * wn[2] : 0;
             const bool use_win = ORDER != 0 && ncell <= a.wcap;
 
@@ -401,7 +401,7 @@ __global__ void __launch_bounds__(BLOCK) k_pair_s1tab(MixedArgs a)
             const float gz = axis_gap(dOz, mI1.z, mJ1.z);
             const float bmax = mI0.w + mJ0.w;
             const float g2 = gx * gx + gy * gy + gz * gz;
-            const bool full = wrapz || g2 <= bmax * bmax * 1.0001f + 1e-30f || coarse_for_gap(dOx, dOy, dOz, mI1, mJ1, g2);
+            const bool full = wrapz || g2 <= bmax * bmax * 1.0001f + 1e-30f || coarse_for_gap(dOx, dOy, dOz, mI1, mJ1, g2, a.guard2);
 
             float phx[IPT], phy[IPT], phz[IPT], plx[IPT], ply[IPT], plz[IPT];
             float fx[IPT], fy[IPT], fz[IPT];
