@@ -166,7 +166,9 @@ int steps_gpu_download_state(double *x, double *v, double *F);
 
 /* Registers `count` independent R^3 realisations; realisation k has n[k]
  * particles whose positions, masses and softening lengths are the host arrays
- * x[k] (double[3 n[k]]), m[k], eps[k]. */
+ * x[k] (double[3 n[k]]), m[k], eps[k]. Velocities start at zero. Registering
+ * the same count and n[] again replaces the data only: the tuned tile shape
+ * and the captured graph of the previous batch are kept. */
 int steps_gpu_batch_set(int count, const int *n, const double *const *x, const double *const *m,
                         const double *const *eps);
 

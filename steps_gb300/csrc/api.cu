@@ -14,6 +14,7 @@
 
 #include "common.cuh"
 #include "context.cuh"
+#include "mixed.cuh"
 
 namespace steps {
 
@@ -427,10 +428,11 @@ int steps_gpu_autotune(const steps_params *p, int id_min, int id_max, int *out)
         float best = 1e30f;
         Shape bestS = keep;
         KParams kp = derive_params(p);
-        const int nvar = kp.topology == STEPS_R3 ? 2 : 1;
+        const int nvar = kp.topology == STEPS_R3 ? 4 : 1;
         for (int v = 0; v < nvar; v++)
         for (auto &s : shapes) {
             if (!shape_supported_for(kp, s[0], s[1])) continue;
+            if (v >= 1 && !r3x2_kernel(s[0], s[1], false, r3x2_occ(v))) continue;
             c.shape.threads = s[0];
             c.shape.ipt = s[1];
             c.shape.jsplit = 0;
@@ -459,7 +461,9 @@ int steps_gpu_set_precision_guard(double ratio)
 int steps_gpu_set_kernel_variant(int variant)
 {
     return guarded([&] {
-        if (variant != 0 && variant != 1) fail(STEPS_E_ARG, "kernel variant must be 0 (scalar) or 1 (packed FP32x2)");
+        if (variant < 0 || variant > 3)
+            fail(STEPS_E_ARG, "kernel variant must be 0 (scalar), 1 (packed FP32x2), 2 or 3 (packed, 768 or 1024 "
+                              "threads per SM)");
         g_ctx.shape.variant = variant;
     });
 }

@@ -108,8 +108,6 @@ __global__ void k_batch_reduce(const double *__restrict__ part, const int2 *__re
     for (int c = 0; c < 3; c++) F[3 * (size_t)o + c] = f[c];
 }
 
-Batch *B() { return ctx().batch; }
-
 // Tile descriptors and the work list for tile size T (host side, once per shape).
 void plan(Batch &b, int threads, int ipt)
 {
@@ -301,19 +299,40 @@ int steps_gpu_batch_set(int count, const int *n, const double *const *x, const d
                 tot += a.n[k];
             }
             if (tot > (1LL << 30)) fail(STEPS_E_ARG, "batch_set: too many particles");
-            batch_release();
-            c.batch = new Batch();
+            // The same realisation sizes as the registered batch: keep its
+            // buffers, tuned tile shape and captured graph, replace the data.
+            const bool same = c.batch && c.batch->count == a.count &&
+                              std::equal(c.batch->n.begin(), c.batch->n.end(), a.n);
+            if (!same) {
+                batch_release();
+                c.batch = new Batch();
+                Batch &b = *c.batch;
+                b.count = a.count;
+                b.n.assign(a.n, a.n + a.count);
+                b.off.resize(a.count);
+                int o = 0;
+                for (int k = 0; k < a.count; k++) { b.off[k] = o; o += a.n[k]; }
+                b.ntot = o;
+                std::vector<uint16_t> rel(b.ntot);
+                for (int k = 0; k < a.count; k++) std::fill(rel.begin() + b.off[k], rel.begin() + b.off[k] + b.n[k], k);
+                b.x.ensure<double>(3 * (size_t)b.ntot);
+                b.m64.ensure<double>(b.ntot);
+                b.eps64.ensure<double>(b.ntot);
+                b.F.ensure<double>(3 * (size_t)b.ntot);
+                b.v.ensure<double>(3 * (size_t)b.ntot);
+                STEPS_CUDA(cudaMemcpyAsync(b.rel.ensure<uint16_t>(b.ntot), rel.data(), sizeof(uint16_t) * b.ntot,
+                                           cudaMemcpyHostToDevice, c.stream));
+                b.bbox.ensure<unsigned long long>(6 * (size_t)a.count);
+                for (int k = 0; k < 2; k++) {
+                    b.ts.keys[k].ensure<unsigned long long>(b.ntot);
+                    b.ts.vals[k].ensure<uint32_t>(b.ntot);
+                }
+                b.counter.ensure<unsigned>(4);
+                b.err.ensure<double>(4);
+                STEPS_CUDA(cudaStreamSynchronize(c.stream));  // rel's host copy goes out of scope
+            }
             Batch &b = *c.batch;
-            b.count = a.count;
-            b.n.assign(a.n, a.n + a.count);
-            b.off.resize(a.count);
-            int o = 0;
-            for (int k = 0; k < a.count; k++) { b.off[k] = o; o += a.n[k]; }
-            b.ntot = o;
-            std::vector<uint16_t> rel(b.ntot);
-            for (int k = 0; k < a.count; k++) std::fill(rel.begin() + b.off[k], rel.begin() + b.off[k] + b.n[k], k);
-            double *dx = b.x.ensure<double>(3 * (size_t)b.ntot);
-            double *dm = b.m64.ensure<double>(b.ntot), *de = b.eps64.ensure<double>(b.ntot);
+            double *dx = b.x.as<double>(), *dm = b.m64.as<double>(), *de = b.eps64.as<double>();
             for (int k = 0; k < a.count; k++) {
                 const size_t off = (size_t)b.off[k];
                 STEPS_CUDA(cudaMemcpyAsync(dx + 3 * off, a.x[k], 3 * sizeof(double) * a.n[k], cudaMemcpyHostToDevice,
@@ -323,18 +342,7 @@ int steps_gpu_batch_set(int count, const int *n, const double *const *x, const d
                 STEPS_CUDA(cudaMemcpyAsync(de + off, a.eps[k], sizeof(double) * a.n[k], cudaMemcpyHostToDevice,
                                            c.stream));
             }
-            STEPS_CUDA(cudaMemsetAsync(b.v.ensure<double>(3 * (size_t)b.ntot), 0, 3 * sizeof(double) * b.ntot,
-                                       c.stream));
-            b.F.ensure<double>(3 * (size_t)b.ntot);
-            STEPS_CUDA(cudaMemcpyAsync(b.rel.ensure<uint16_t>(b.ntot), rel.data(), sizeof(uint16_t) * b.ntot,
-                                       cudaMemcpyHostToDevice, c.stream));
-            b.bbox.ensure<unsigned long long>(6 * (size_t)a.count);
-            for (int k = 0; k < 2; k++) {
-                b.ts.keys[k].ensure<unsigned long long>(b.ntot);
-                b.ts.vals[k].ensure<uint32_t>(b.ntot);
-            }
-            b.counter.ensure<unsigned>(4);
-            b.err.ensure<double>(4);
+            STEPS_CUDA(cudaMemsetAsync(b.v.as<double>(), 0, 3 * sizeof(double) * b.ntot, c.stream));
             STEPS_CUDA(cudaStreamSynchronize(c.stream));
         },
         &args);

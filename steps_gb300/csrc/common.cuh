@@ -85,7 +85,7 @@ struct Shape {
     int threads = 128;
     int ipt = 2;
     int jsplit = 0;
-    int variant = 0;  // R^3: 0 scalar FP32 pair loop, 1 packed FP32x2 pair loop
+    int variant = 0;  // R^3: 0 scalar FP32 pair loop; 1, 2, 3 packed FP32x2 (0, 768, 1024 threads/SM asked)
     float guard = 30.0f;  // tile-pair scale / gap above which the double-float path runs
 };
 

@@ -30,6 +30,8 @@ struct MixedArgs {
     double *part;       // [S][nit*T][3]
     size_t part_stride; // nit*T*3
     float L, halfL, cutL;
+    float L_lo, halfL_lo;  // L - fl(L), L/2 - fl(L/2): the FP32 residuals of the period
+    float wrap_tol;     // |d| this close to L/2 takes the nearest-image decision on an exact d
     float cut_tol;      // |dz + mL| this close to cutL is re-decided on an exact dz
     float guard2;       // square of the precision guard ratio (coarse_for_gap)
     int emax;
@@ -106,6 +108,39 @@ __device__ __forceinline__ void frame_split(float xh, float xl, float dO, float 
     pl = (e - eO) + xl;
 }
 
+// Moves J's centre to its image nearest I's along one axis: d_O + e_O
+// becomes d_O + e_O - k L with k = rint(d_O / L). The subtraction's rounding
+// and the FP32 residual of L go into e_O, so the frame change stays exact.
+__device__ __forceinline__ void shift_frame(float &dO, float &eO, float L, float L_lo)
+{
+    const float k = rintf(dO / L);
+    if (k != 0.0f) {
+        float e;
+        dO = two_diff(dO, k * L, e);
+        eO = (eO + e) - k * L_lo;
+    }
+}
+
+// Nearest image along one axis, |d| > L/2 -> d - sign(d) L
+// (StePS/src/forces.cc:812-817), for the double-float separation
+// d = (q + ql) - (ph + pl) whose FP32 rounding is d. Within wrap_tol of L/2
+// the decision is taken on the unrounded sum, so FP32 rounding never picks
+// another image than the FP64 reference (a flip reverses the pair's force).
+__device__ __forceinline__ float nearest_image(float d, float q, float ph, float ql, float pl, float L, float halfL,
+                                               float halfL_lo, float wrap_tol)
+{
+    const float ad = fabsf(d);
+    bool w = ad > halfL;
+    if (fabsf(ad - halfL) < wrap_tol) {
+        float e;
+        const float s = two_diff(q, ph, e);
+        const float t = e + (ql - pl);
+        // |s + t| - L/2 with |s| - fl(L/2) exact (Sterbenz); its sign is the decision.
+        w = (fabsf(s) - halfL) + (copysignf(1.0f, s) * t - halfL_lo) > 0.0f;
+    }
+    return w ? d - copysignf(L, d) : d;
+}
+
 // Lower bound of |d| over the separations of two boxes along one axis.
 __device__ __forceinline__ float axis_gap(float dO, float hI, float hJ) { return fmaxf(fabsf(dO) - hI - hJ, 0.0f); }
 
@@ -117,8 +152,11 @@ using KernelFn = void (*)(MixedArgs);
 // table arguments (FP32 table copy, grid geometry).
 mixed::KernelFn t3_kernel(const KParams &kp, int threads, int ipt, size_t *dyn_smem);
 void t3_args(mixed::MixedArgs &a, const KParams &kp, const Tables &tb, cudaStream_t st);
-// pair_r3x2.cu: R^3 kernel on packed FP32 pairs.
-mixed::KernelFn r3x2_kernel(int threads, int ipt, bool list = false);
+// pair_r3x2.cu: R^3 kernel on packed FP32 pairs; occ = 0, 768 or 1024
+// resident threads per SM requested from the register allocator.
+mixed::KernelFn r3x2_kernel(int threads, int ipt, bool list = false, int occ = 0);
+// Resident-thread request of a packed R^3 kernel variant (1, 2, 3).
+inline int r3x2_occ(int variant) { return variant == 2 ? 768 : variant == 3 ? 1024 : 0; }
 // S1xR2 with the (rho, z) table (IS_PERIODIC >= 2, no explicit images).
 mixed::KernelFn s1tab_kernel(const KParams &kp, int threads, int ipt);
 void s1tab_args(mixed::MixedArgs &a, const KParams &kp, const Tables &tb, cudaStream_t st);

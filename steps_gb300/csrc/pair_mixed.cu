@@ -226,7 +226,9 @@ __global__ void __launch_bounds__(BLOCK, KIND == K_R3 && IPT == 1 ? 1024 / BLOCK
                             const float rho2 = fmaf(dx, dx, dy * dy);
                             int mlo = -a.emax, mhi = a.emax;
                             if (KIND == K_S1_GEN && a.nearest) {
-                                dz = fabsf(dz) > a.halfL ? dz - copysignf(a.L, dz) : dz;
+                                if (!self)
+                                    dz = nearest_image(dz, q.z, phz[k], ql.z, plz[k], a.L, a.halfL, a.halfL_lo,
+                                                       a.wrap_tol);
                                 mlo = mhi = 0;
                             }
                             float sw = 0.0f, swz = 0.0f;
@@ -353,10 +355,10 @@ void forces_mixed(const KParams &kp, const Tables &tb, const double *x, const do
     const int T = threads * ipt;
     size_t dyn = 0;
     const bool s1tab = kp.topology == STEPS_S1R2 && kp.is_periodic >= 2 && !kp.s1r2_images;
-    const bool packed = kp.topology == STEPS_R3 && c.shape.variant == 1;
+    const bool packed = kp.topology == STEPS_R3 && c.shape.variant >= 1;
     KernelFn fn = kp.topology == STEPS_T3 ? t3_kernel(kp, threads, ipt, &dyn)
                   : s1tab              ? s1tab_kernel(kp, threads, ipt)
-                  : packed             ? r3x2_kernel(threads, ipt)
+                  : packed             ? r3x2_kernel(threads, ipt, false, r3x2_occ(c.shape.variant))
                                        : select_kernel(kp, threads, ipt);
     if (!fn) fail(STEPS_E_ARG, "mixed precision: unsupported topology/mode or kernel shape");
 
@@ -420,6 +422,9 @@ void forces_mixed(const KParams &kp, const Tables &tb, const double *x, const do
     a.halfL = (float)kp.halfL;
     a.cutL = (float)kp.cutL;
     a.cut_tol = (float)(kp.cutL * 1e-5);
+    a.L_lo = (float)(kp.L - (double)a.L);
+    a.halfL_lo = (float)(kp.halfL - (double)a.halfL);
+    a.wrap_tol = (float)(kp.halfL * 1e-5);
     a.guard2 = c.shape.guard * c.shape.guard;
     a.emax = kp.emax;
     a.nearest = kp.topology == STEPS_S1R2 && kp.is_periodic < 2;

@@ -78,7 +78,7 @@ __device__ __forceinline__ void stage_soa(const MixedArgs &a, int J, float *sx, 
 }
 
 template <int BLOCK, int IPT, bool LIST>
-__global__ void __launch_bounds__(BLOCK) k_pair_r3x2(MixedArgs a)
+__device__ __forceinline__ void r3x2_body(const MixedArgs &a)
 {
     constexpr int T = BLOCK * IPT;
     __shared__ __align__(16) float sx[2][4 * T];  // X[T], Y[T], Z[T], M[T]
@@ -257,12 +257,33 @@ __global__ void __launch_bounds__(BLOCK) k_pair_r3x2(MixedArgs a)
     }
 }
 
+template <int BLOCK, int IPT, bool LIST>
+__global__ void __launch_bounds__(BLOCK) k_pair_r3x2(MixedArgs a)
+{
+    r3x2_body<BLOCK, IPT, LIST>(a);
+}
+
+// The same kernel with OCC resident threads per SM asked of the register
+// allocator (65536 / OCC registers a thread): more warps to hide the FP32x2
+// and MUFU latencies, at the price of spills for the larger tiles.
+template <int BLOCK, int IPT, int OCC>
+__global__ void __launch_bounds__(BLOCK, OCC / BLOCK) k_pair_r3x2_occ(MixedArgs a)
+{
+    r3x2_body<BLOCK, IPT, false>(a);
+}
+
 }  // namespace
 
-KernelFn r3x2_kernel(int threads, int ipt, bool list)
+KernelFn r3x2_kernel(int threads, int ipt, bool list, int occ)
 {
-#define STEPS_SHAPE(B, P) \
-    if (threads == B && ipt == P) return list ? k_pair_r3x2<B, P, true> : k_pair_r3x2<B, P, false>;
+#define STEPS_SHAPE(B, P)                                                         \
+    if (threads == B && ipt == P) {                                              \
+        if (list) return occ == 0 ? k_pair_r3x2<B, P, true> : nullptr;          \
+        if (occ == 0) return k_pair_r3x2<B, P, false>;                          \
+        if (occ == 768) return k_pair_r3x2_occ<B, P, 768>;                      \
+        if (occ == 1024) return k_pair_r3x2_occ<B, P, 1024>;                    \
+        return nullptr;                                                          \
+    }
     STEPS_SHAPE(64, 1) STEPS_SHAPE(64, 2) STEPS_SHAPE(64, 4)
     STEPS_SHAPE(128, 1) STEPS_SHAPE(128, 2) STEPS_SHAPE(128, 4)
     STEPS_SHAPE(256, 1) STEPS_SHAPE(256, 2)

@@ -108,8 +108,8 @@ __global__ void __launch_bounds__(BLOCK) k_pair_t3(MixedArgs a)
             float uc[3];
 #pragma unroll
             for (int ax3 = 0; ax3 < 3; ax3++) {
-                dO[ax3] -= L * rintf(dO[ax3] / L);  // nearest image of J's centre
-                wrap[ax3] = fabsf(dO[ax3]) + hs[ax3] > halfL;
+                shift_frame(dO[ax3], eO[ax3], L, a.L_lo);  // nearest image of J's centre
+                wrap[ax3] = fabsf(dO[ax3]) + hs[ax3] > halfL - a.wrap_tol;  // conservative by wrap_tol
                 const float g = fmaxf(fabsf(dO[ax3]) - hs[ax3], 0.0f);
                 g2 += g * g;
                 if (ORDER != 0) {
@@ -125,7 +125,11 @@ __global__ void __launch_bounds__(BLOCK) k_pair_t3(MixedArgs a)
             const float bmax = mI0.w + mJ0.w;
             const bool full = g2 <= bmax * bmax * 1.0001f + 1e-30f || wrap[0] || wrap[1] || wrap[2] ||
                               coarse_for_gap(dO[0], dO[1], dO[2], mI1, mJ1, g2, a.guard2);
-            const int ncell = ORDER != 0 ? wn[0] * wn[1] * wn[2] : 0;
+            // Window strides are odd so that neighbouring cells fall in
+            // different shared-memory banks; cells past wn[] are padding.
+            const int sy = ORDER != 0 ? (wn[2] | 1) : 0;
+            const int sx = ORDER != 0 ? ((wn[1] * sy) | 1) : 0;
+            const int ncell = ORDER != 0 ? wn[0] * sx : 0;
             const bool use_win = ORDER != 0 && ncell <= a.wcap;
 
             if (J + 1 < J1) {
@@ -136,9 +140,10 @@ __global__ void __launch_bounds__(BLOCK) k_pair_t3(MixedArgs a)
             }
             if (use_win) {
                 for (int cidx = tid; cidx < ncell; cidx += BLOCK) {
-                    const int cz = cidx % wn[2];
-                    const int cy = (cidx / wn[2]) % wn[1];
-                    const int cx = cidx / (wn[2] * wn[1]);
+                    const int cx = cidx / sx;
+                    const int rem = cidx - cx * sx;
+                    const int cy = rem / sy;
+                    const int cz = rem - cy * sy;
                     const int gx = pmod(w0[0] + cx, a.ng), gy = pmod(w0[1] + cy, a.ng), gz = pmod(w0[2] + cz, a.ng);
                     win[cidx] = __ldg(a.t3f + ((size_t)gx * a.ng + gy) * a.ng + gz);
                 }
@@ -161,7 +166,6 @@ __global__ void __launch_bounds__(BLOCK) k_pair_t3(MixedArgs a)
             const float *seb = se[buf];
             const uint32_t *sidb = sid[buf];
             const float4 *sresb = sres[buf];
-            const int sy = ORDER != 0 ? wn[2] : 0, sx = ORDER != 0 ? wn[1] * wn[2] : 0;
 
 #pragma unroll 2
             for (int jj = 0; jj < T; ++jj) {
@@ -183,9 +187,12 @@ __global__ void __launch_bounds__(BLOCK) k_pair_t3(MixedArgs a)
                         dz = q.z - pz[k];
                     }
                     float nx = dx, ny = dy, nz = dz;
-                    if (wrap[0]) nx = fabsf(nx) > halfL ? nx - copysignf(L, nx) : nx;
-                    if (wrap[1]) ny = fabsf(ny) > halfL ? ny - copysignf(L, ny) : ny;
-                    if (wrap[2]) nz = fabsf(nz) > halfL ? nz - copysignf(L, nz) : nz;
+                    if (full && !self) {  // wrapped axes are full-path tile pairs
+                        const float4 ql = sresb[jj];
+                        if (wrap[0]) nx = nearest_image(dx, q.x, phx[k], ql.x, plx[k], L, halfL, a.halfL_lo, a.wrap_tol);
+                        if (wrap[1]) ny = nearest_image(dy, q.y, phy[k], ql.y, ply[k], L, halfL, a.halfL_lo, a.wrap_tol);
+                        if (wrap[2]) nz = nearest_image(dz, q.z, phz[k], ql.z, plz[k], L, halfL, a.halfL_lo, a.wrap_tol);
+                    }
                     const float r2 = fmaf(nx, nx, fmaf(ny, ny, nz * nz));
                     const float ri = rsqrt_mufu(r2);
                     float w = ri * ri * ri;
@@ -394,9 +401,9 @@ __global__ void __launch_bounds__(BLOCK) k_pair_s1tab(MixedArgs a)
             float eOx, eOy, eOz;
             const float dOx = two_diff(mJ0.x, mI0.x, eOx), dOy = two_diff(mJ0.y, mI0.y, eOy);
             float dOz = two_diff(mJ0.z, mI0.z, eOz);
-            dOz -= L * rintf(dOz / L);  // nearest image of J's centre along z
+            shift_frame(dOz, eOz, L, a.L_lo);  // nearest image of J's centre along z
             const float hz = mI1.z + mJ1.z;
-            const bool wrapz = fabsf(dOz) + hz > halfL;
+            const bool wrapz = fabsf(dOz) + hz > halfL - a.wrap_tol;
             const float gx = axis_gap(dOx, mI1.x, mJ1.x), gy = axis_gap(dOy, mI1.y, mJ1.y);
             const float gz = axis_gap(dOz, mI1.z, mJ1.z);
             const float bmax = mI0.w + mJ0.w;
@@ -427,7 +434,7 @@ __global__ void __launch_bounds__(BLOCK) k_pair_s1tab(MixedArgs a)
                     const float dx = self ? 0.0f : (q.x - phx[k]) + (ql.x - plx[k]);
                     const float dy = self ? 0.0f : (q.y - phy[k]) + (ql.y - ply[k]);
                     float dz = self ? 0.0f : (q.z - phz[k]) + (ql.z - plz[k]);
-                    if (wrapz) dz = fabsf(dz) > halfL ? dz - copysignf(L, dz) : dz;
+                    if (wrapz && !self) dz = nearest_image(dz, q.z, phz[k], ql.z, plz[k], L, halfL, a.halfL_lo, a.wrap_tol);
                     const float rho2 = fmaf(dx, dx, dy * dy);
                     const float r2 = fmaf(dz, dz, rho2);
                     const float ri = rsqrt_mufu(r2);

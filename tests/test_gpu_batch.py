@@ -43,6 +43,10 @@ def test_batch_graph_and_plain_match_oracle(engine, port):
         engine.batch_set([s.x for s in sets], [s.m for s in sets], [s.eps for s in sets])
         engine.batch_run(p, S.MIXED, 2, DT, graph=False)
         plain = [engine.batch_get(k) for k in range(len(sets))]
+        # same sizes registered again: new data, the tuned plan and graph are reused
+        engine.batch_set([s.x for s in sets], [s.m for s in sets], [s.eps for s in sets])
+        engine.batch_run(p, S.MIXED, 2, DT, graph=True)
+        again = [engine.batch_get(k) for k in range(len(sets))]
     finally:
         engine.set_variant(0)
     for k, ps in enumerate(sets):
@@ -52,6 +56,8 @@ def test_batch_graph_and_plain_match_oracle(engine, port):
             assert err_stats(F, Fo)["p99"] < 1e-5, (k, name)
             assert err_stats(v, vo)["p99"] < 1e-5, (k, name)
         assert rel_err(graph[k][2], plain[k][2]).max() < 1e-5
+        for a, b in zip(again[k], graph[k]):
+            assert np.array_equal(a, b), k  # deterministic reduction order
         xo4, vo4, Fo4 = oracle_run(port, ps, 4)
         assert err_stats(graph4[k][2], Fo4)["p99"] < 1e-5, k
         assert np.abs(graph4[k][0] - xo4).max() < 1e-9 * (1 + np.abs(xo4).max()), k

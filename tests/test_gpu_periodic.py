@@ -177,3 +177,59 @@ def test_t3_mixed_shapes_and_workload_table(engine, port, order):
         st = err_stats(engine.forces(ps.x, p, S.MIXED), F64)
         assert st["p99"] < MIXED_P99, (threads, ipt, st)
     engine.set_tuning(128, 2, 0)
+
+
+def half_box_pairs(x, L, axes, seed, npairs):
+    """Places particle 2p+1 at particle 2p's position shifted by L/2 + delta
+    along one axis, delta within a few FP32 ulps of L/2: the reference's
+    nearest-image test |d| > L/2 then sits inside FP32 rounding."""
+    rng = np.random.default_rng(seed)
+    x = x.copy()
+    ulp = np.spacing(np.float32(L / 2))
+    for p in range(npairs):
+        i, j = 2 * p, 2 * p + 1
+        ax = axes[p % len(axes)]
+        x[j] = x[i]
+        x[j, ax] = np.mod(x[i, ax] + L / 2 + rng.uniform(-3.0, 3.0) * ulp, L)
+    return x
+
+
+@pytest.mark.parametrize("isp", [1, 2])
+def test_t3_nearest_image_at_half_box(engine, isp):
+    """Pairs at |dx| = L/2 within FP32 rounding along every axis: mixed takes
+    the same image as the FP64 kernel (a different one reverses the pair's
+    direct force, ~1e-2 of these particles' forces)."""
+    g = golden("t3_o2")
+    ng, L = int(g["ngrid"]), float(g["L"])
+    rng = np.random.default_rng(5)
+    n = 4096
+    x = half_box_pairs(rng.uniform(0.0, L, (n, 3)), L, (0, 1, 2), 6, 1024)
+    m = np.full(n, 1.0 / n)
+    eps = np.full(n, 0.01 * L / 16)
+    engine.set_particles(m, eps)
+    engine.set_table_t3(g["table"], ng)
+    p = S.params(S.T3, is_periodic=isp, L=L, rsim=L / 2, ewald_order=2)
+    F64 = engine.forces(x, p, S.FP64)
+    e = rel_err(engine.forces(x, p, S.MIXED), F64)
+    assert np.percentile(e[:2048], 99) < MIXED_P99 and np.percentile(e, 99) < MIXED_P99, (
+        np.percentile(e[:2048], [50, 99, 100]))
+
+
+@pytest.mark.parametrize("mode", ["nearest", "table"])
+def test_s1r2_nearest_image_at_half_period(engine, mode):
+    """The same along the periodic z axis of S1xR2: IS_PERIODIC = 1 (nearest
+    image only) and the (rho, z) table mode, both wrap dz at L/2."""
+    g = golden("s1r2_table_o2")
+    L = float(g["L"])
+    n = g["x"].shape[0] - g["x"].shape[0] % 2
+    x = half_box_pairs(g["x"][:n], L, (2,), 8, n // 4)
+    engine.set_particles(g["m"][:n], g["eps"][:n])
+    if mode == "table":
+        nrho, nz = (int(v) for v in g["shape"])
+        engine.set_table_s1r2(g["table"], nrho, nz)
+        p = s1_params(g, 2, images=0, order=2)
+    else:
+        p = s1_params(g, 1)
+    F64 = engine.forces(x, p, S.FP64)
+    e = rel_err(engine.forces(x, p, S.MIXED), F64)
+    assert np.percentile(e[:n // 2], 99) < MIXED_P99, np.percentile(e[:n // 2], [50, 99, 100])
