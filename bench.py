@@ -43,6 +43,7 @@ UNIT = "pairs/s"
 # Ewald table of the T^3 workload: Ng = 63, alpha = 2/L, real images |r+nL| <= 2L
 # (index radius 3), k vectors |k| <= 5 (2 pi / L) (index radius 6).
 T3_NG = 63
+LOOPS = ["fp32", "fp32x2", "fp32x2 (768 threads/SM)", "fp32x2 (1024 threads/SM)"]
 
 
 def parse():
@@ -56,10 +57,14 @@ def parse():
     ap.add_argument("--order", type=int, default=2, help="T^3 interpolation order (2 or 4)")
     ap.add_argument("--n", type=int, default=0, help="override the particle count (small profiling cases)")
     ap.add_argument("--fp64-sample", type=int, default=16384, help="i particles timed with the FP64 kernel")
-    ap.add_argument("--cpu-sample", type=int, default=1024, help="i particles in the CPU baseline sample")
+    ap.add_argument("--cpu-sample", type=int, default=0,
+                    help="i particles in the CPU baseline sample (0: sized for --cpu-seconds)")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target CPU time of one baseline sample")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-autotune", action="store_true")
-    ap.add_argument("--variant", type=int, default=-1, help="R^3 pair loop without autotuning: 0 fp32, 1 fp32x2")
+    ap.add_argument("--variant", type=int, default=-1,
+                    help="R^3 pair loop without autotuning: 0 fp32, 1 fp32x2, 2/3 fp32x2 at 768/1024 threads per SM")
+    ap.add_argument("--shape", default="", help="kernel shape THREADSxIPT without autotuning, e.g. 128x1")
     return ap.parse_args()
 
 
@@ -166,9 +171,11 @@ class ClockSampler:
                 "samples": len(self.rows)}
 
 
-def cpu_baseline(ps, p, sample: int, threads: int, table=None, ngrid=0):
+def cpu_baseline(ps, p, sample: int, threads: int, table=None, ngrid=0, seconds: float = 10.0):
     """The reference algorithm on the host cores: the plain-C oracle (OpenMP
-    over i, sequential j, per-pair atomics, as StePS/src/forces.cc)."""
+    over i, sequential j, per-pair atomics, as StePS/src/forces.cc), timed on
+    the i range [N/2, N/2 + sample) against all N j. sample <= 0 sizes the
+    range from a short calibration run so that it takes about `seconds`."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
 
@@ -177,8 +184,19 @@ def cpu_baseline(ps, p, sample: int, threads: int, table=None, ngrid=0):
     s = port.system(tp, ps.m, ps.eps, pyoracle.make_params(p.is_periodic, p.L, p.rsim), table=table, ngrid=ngrid,
                     order=p.ewald_order)
     lo = ps.n // 2
-    hi = min(ps.n - 1, lo + sample - 1)
-    port.forces(s, ps.x, lo, min(hi, lo + 7))  # warm
+    probe = min(max(threads, 8), ps.n - lo)
+    while True:  # warm-up and calibration: grow the probe until it takes 0.25 s
+        t0 = time.perf_counter()
+        port.forces(s, ps.x, lo, lo + probe - 1)
+        dt = time.perf_counter() - t0
+        if dt >= 0.25 or probe >= ps.n - lo:
+            break
+        probe = min(4 * probe, ps.n - lo)
+    rate0 = probe * ps.n / max(dt, 1e-9)
+    if sample <= 0:
+        sample = int(rate0 * seconds / ps.n)
+    sample = max(8, min(sample, ps.n - lo))
+    hi = lo + sample - 1
     t0 = time.perf_counter()
     port.forces(s, ps.x, lo, hi)
     dt = time.perf_counter() - t0
@@ -201,12 +219,14 @@ def run_reference(args, ws, rank):
     ps, p, flops, desc, table = workload(args)
     tab, ng = host_table(table) if table else (None, 0)
     threads = os.cpu_count() or 1
-    sample = max(8, args.cpu_sample // (8 if p.topology != 0 else 1))
     for _ in range(max(args.warmup, 0)):
-        cpu_baseline(ps, p, max(8, sample // 8), threads, tab, ng)
-    rates = [cpu_baseline(ps, p, sample, threads, tab, ng)[0] for _ in range(args.steps)]
-    v = float(np.median(rates))
-    smp = f"{sample} i particles x all {ps.n} j per step (force cost is linear in the i range)"
+        cpu_baseline(ps, p, 0, threads, tab, ng, seconds=args.cpu_seconds / 8)
+    runs = [cpu_baseline(ps, p, args.cpu_sample, threads, tab, ng, seconds=args.cpu_seconds)
+            for _ in range(args.steps)]
+    v = float(np.median([r[0] for r in runs]))
+    sample = runs[0][3]
+    smp = (f"{sample} i particles x all {ps.n} j per step, about {args.cpu_seconds:g} s of CPU work each "
+           "(force cost is linear in the i range)")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": float(sample * ps.n / v * 1e3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
@@ -229,7 +249,11 @@ def run_ours(args, ws, rank, local, dist):
     f32_peak, f64_peak = eng.measure_peaks()
     if args.variant >= 0:
         eng.set_variant(args.variant)
-    shape = None if (args.no_autotune or args.variant >= 0) else eng.autotune(p)
+    if args.shape:
+        th, ipt = (int(v) for v in args.shape.split("x"))
+        eng.set_tuning(th, ipt, 0)
+    fixed = args.no_autotune or args.variant >= 0 or bool(args.shape)
+    shape = None if fixed else eng.autotune(p)
 
     for _ in range(args.warmup):
         eng.forces_resident(p, S.MIXED)
@@ -293,8 +317,8 @@ def run_ours(args, ws, rank, local, dist):
         "config": {"workload": desc + ", one full force evaluation per step", "n": n, "pairs_per_step": pairs_step,
                    "parallelism": "one independent realisation per GPU" if ws > 1 else "1 GPU",
                    "l2": "512 MB flush between steps", "precision": "mixed",
-                   "kernel_shape": ({"threads": shape[0], "ipt": shape[1], "pair_loop": ["fp32", "fp32x2"][shape[2]]}
-                                    if shape else "default 128x2 fp32"),
+                   "kernel_shape": ({"threads": shape[0], "ipt": shape[1], "pair_loop": LOOPS[shape[2]]}
+                                    if shape else (args.shape or "128x2") + " " + LOOPS[max(args.variant, 0)]),
                    "prep_ms": float(np.mean(prep_ms))},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(ps.x.nbytes),
                 "d2h_bytes_per_step": int(F_host.nbytes), "ms_per_step": e2e_t * 1e3},
@@ -397,8 +421,7 @@ def main():
     if rank == 0:
         threads = os.cpu_count() or 1
         tab, ng = host_table(table) if table else (None, 0)
-        sample = max(8, args.cpu_sample // (8 if p.topology != 0 else 1))
-        rate, dt, pairs, ni = cpu_baseline(ps, p, sample, threads, tab, ng)
+        rate, dt, pairs, ni = cpu_baseline(ps, p, args.cpu_sample, threads, tab, ng, seconds=args.cpu_seconds)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                                 "sample": f"{ni} i particles x all {ps.n} j ({dt:.1f} s of CPU work)"}
         print(json.dumps(line), flush=True)

@@ -193,15 +193,25 @@ int steps_gpu_set_tuning(int threads, int ipt, int jsplit);
  * rounding; the autotuner picks between them. */
 int steps_gpu_set_kernel_variant(int variant);
 
+/* T^3 mixed precision: capacity, in table cells (16 bytes each), of the
+ * shared-memory window of the Ewald table that each block stages per tile
+ * pair. Tile pairs whose window does not fit read the table through L1/L2.
+ * 0 disables the window. Default 1024; at most STEPS_T3_WINDOW_MAX.
+ * steps_gpu_autotune searches 0, 1024 and 2048 for trilinear tables and
+ * uses 2048 for tricubic ones. */
+#define STEPS_T3_WINDOW_MAX 12288
+int steps_gpu_set_t3_window(int cells);
+
 /* Mixed precision: tile pairs whose coordinate scale (centre distance plus
  * half extents) exceeds `ratio` times their box gap run the double-float
  * near-field path instead of the FP32 far-field loop. Lower = more accurate
  * and slower. Range [1, 1e6]. */
 int steps_gpu_set_precision_guard(double ratio);
 
-/* Times every supported mixed-precision shape (and, for R^3, both pair-loop
- * variants) on the resident particles for the given topology and keeps the
- * fastest; writes threads, ipt, variant to out[3]. */
+/* Times every supported mixed-precision shape on the resident particles for
+ * the given topology -- for R^3 with each pair-loop variant, for trilinear
+ * T^3 with each table-window size -- and keeps the fastest; writes threads,
+ * ipt, variant to out[3]. One evaluation per candidate. */
 int steps_gpu_autotune(const steps_params *p, int id_min, int id_max, int *out);
 
 /* Number of kernels this library has launched since init. */

@@ -214,6 +214,9 @@ class Engine:
         self.lib.steps_gpu_set_precision_guard.argtypes = [C.c_double]
         self._check(self.lib.steps_gpu_set_precision_guard(float(ratio)))
 
+    def set_t3_window(self, cells: int):
+        self._check(self.lib.steps_gpu_set_t3_window(int(cells)))
+
     def set_variant(self, variant: int):
         self._check(self.lib.steps_gpu_set_kernel_variant(int(variant)))
 

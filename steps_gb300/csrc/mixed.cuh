@@ -141,6 +141,18 @@ __device__ __forceinline__ float nearest_image(float d, float q, float ph, float
     return w ? d - copysignf(L, d) : d;
 }
 
+// The S1xR2 image cut |dz + sh| <= cutL (StePS/src/forces.cc:1274) decided on
+// the double-float dz = (qz + qlz) - (phz + plz): a hard cut, so within FP32
+// rounding of it the rounded dz could decide differently than FP64.
+__device__ __forceinline__ bool cut_in_exact(float qz, float qlz, float phz, float plz, float sh, float cutL)
+{
+    float e1, e2;
+    const float s1 = two_diff(qz, phz, e1);
+    const float hh = two_diff(s1, -sh, e2);
+    const float tail = e2 + (e1 + (qlz - plz));
+    return (fabsf(hh) - cutL) + copysignf(1.0f, hh) * tail <= 0.0f;
+}
+
 // Lower bound of |d| over the separations of two boxes along one axis.
 __device__ __forceinline__ float axis_gap(float dO, float hI, float hJ) { return fmaxf(fabsf(dO) - hI - hJ, 0.0f); }
 

@@ -93,14 +93,15 @@ __global__ void __launch_bounds__(BLOCK, KIND == K_R3 && IPT == 1 ? 1024 / BLOCK
             // exact): the i particles' positions in J's frame then carry
             // ~1e-7 of |x_i - c_J| whatever the size of the i tile.
             float eOx, eOy, eOz;
-            const float dOx = two_diff(mJ0.x, mI0.x, eOx), dOy = two_diff(mJ0.y, mI0.y, eOy),
-                        dOz = two_diff(mJ0.z, mI0.z, eOz);
+            const float dOx = two_diff(mJ0.x, mI0.x, eOx), dOy = two_diff(mJ0.y, mI0.y, eOy);
+            float dOz = two_diff(mJ0.z, mI0.z, eOz);
             const float bmax = mI0.w + mJ0.w;
             const float bmax2 = bmax * bmax * 1.0001f + 1e-30f;
             const float gx = axis_gap(dOx, mI1.x, mJ1.x), gy = axis_gap(dOy, mI1.y, mJ1.y);
 
-            bool full;  // near-field / mixed-cut tile pair: run every test per pair
+            bool full;  // near-field tile pair: softening and every test per pair
             float off[NIMG];
+            unsigned strad = 0u;  // S1 images straddling the cut over this tile pair
             if (KIND == K_R3) {
                 const float gz = axis_gap(dOz, mI1.z, mJ1.z);
                 const float g2 = gx * gx + gy * gy + gz * gz;
@@ -108,26 +109,37 @@ __global__ void __launch_bounds__(BLOCK, KIND == K_R3 && IPT == 1 ? 1024 / BLOCK
             } else if (KIND == K_S1_IMG) {
                 // Range of dz over the tile pair, then per image m: entirely
                 // inside the cut (offset m L), entirely outside (offset 1e18,
-                // whose 1/r^3 underflows to 0), or straddling (full path).
+                // whose 1/r^3 underflows to 0), or straddling (offset m L and
+                // a per-pair cut test, bit m of `strad`).
                 const float hz = mI1.z + mJ1.z;
                 const float lo = dOz - hz, hi = dOz + hz;
                 const float g2xy = gx * gx + gy * gy;
-                bool mixed = false, near = false;
+                bool near = false;
                 float g2min = 3.0e38f;
                 const float cin = a.cutL * (1.0f - 1e-6f), cout = a.cutL * (1.0f + 1e-6f);
+                strad = 0u;
 #pragma unroll
                 for (int m = 0; m < NIMG; m++) {
                     const float sh = (float)(m - EMAX) * a.L;
                     const float l = lo + sh, h = hi + sh;
                     const bool in = fmaxf(fabsf(l), fabsf(h)) <= cin;
                     const bool out = l > cout || h < -cout;
-                    mixed |= !(in || out);
-                    off[m] = in ? sh : 1e18f;
+                    strad |= (in || out) ? 0u : 1u << m;
+                    off[m] = out ? 1e18f : sh;
                     const float gz = (l <= 0.0f && h >= 0.0f) ? 0.0f : fminf(fabsf(l), fabsf(h));
                     near |= !out && (g2xy + gz * gz <= bmax2);
                     if (!out) g2min = fminf(g2min, g2xy + gz * gz);
                 }
-                full = mixed || near || coarse_for_gap(dOx, dOy, dOz, mI1, mJ1, g2min, a.guard2);
+                full = near || coarse_for_gap(dOx, dOy, dOz, mI1, mJ1, g2min, a.guard2);
+            } else if (a.nearest) {
+                // S1xR2 nearest image along z: J's centre moves to the image
+                // nearest I's; tile pairs whose dz range stays inside +-L/2 need
+                // no per-pair wrap and take the R^3 far path.
+                shift_frame(dOz, eOz, a.L, a.L_lo);
+                const float gz = axis_gap(dOz, mI1.z, mJ1.z);
+                const float g2 = gx * gx + gy * gy + gz * gz;
+                full = fabsf(dOz) + mI1.z + mJ1.z > a.halfL - a.wrap_tol || g2 <= bmax2 ||
+                       coarse_for_gap(dOx, dOy, dOz, mI1, mJ1, g2, a.guard2);
             } else {
                 full = true;
             }
@@ -147,7 +159,7 @@ __global__ void __launch_bounds__(BLOCK, KIND == K_R3 && IPT == 1 ? 1024 / BLOCK
             const float4 *sresb = sres[buf];
 
             if (!full) {
-                if (KIND == K_R3) {
+                if (KIND == K_R3 || KIND == K_S1_GEN) {  // K_S1_GEN: nearest-image tile pairs only
 #pragma unroll 8
                     for (int jj = 0; jj < T; ++jj) {
                         const float4 q = spb[jj];
@@ -163,26 +175,59 @@ __global__ void __launch_bounds__(BLOCK, KIND == K_R3 && IPT == 1 ? 1024 / BLOCK
                         }
                     }
                 } else if (KIND == K_S1_IMG) {
+                    if (strad == 0u) {  // every image entirely in or out of the cut
 #pragma unroll 2
-                    for (int jj = 0; jj < T; ++jj) {
-                        const float4 q = spb[jj];
+                        for (int jj = 0; jj < T; ++jj) {
+                            const float4 q = spb[jj];
 #pragma unroll
-                        for (int k = 0; k < IPT; k++) {
-                            const float dx = q.x - px[k], dy = q.y - py[k], dz = q.z - pz[k];
-                            const float rho2 = fmaf(dx, dx, dy * dy);
-                            float sw = 0.0f, swz = 0.0f;
+                            for (int k = 0; k < IPT; k++) {
+                                const float dx = q.x - px[k], dy = q.y - py[k], dz = q.z - pz[k];
+                                const float rho2 = fmaf(dx, dx, dy * dy);
+                                float sw = 0.0f, swz = 0.0f;
 #pragma unroll
-                            for (int m = 0; m < NIMG; m++) {
-                                const float dzm = dz + off[m];
-                                const float ri = rsqrt_mufu(fmaf(dzm, dzm, rho2));
-                                const float ri3 = ri * ri * ri;
-                                sw += ri3;
-                                swz = fmaf(ri3, dzm, swz);
+                                for (int m = 0; m < NIMG; m++) {
+                                    const float dzm = dz + off[m];
+                                    const float ri = rsqrt_mufu(fmaf(dzm, dzm, rho2));
+                                    const float ri3 = ri * ri * ri;
+                                    sw += ri3;
+                                    swz = fmaf(ri3, dzm, swz);
+                                }
+                                const float t = q.w * sw;
+                                fx[k] = fmaf(t, dx, fx[k]);
+                                fy[k] = fmaf(t, dy, fy[k]);
+                                fz[k] = fmaf(q.w, swz, fz[k]);
                             }
-                            const float t = q.w * sw;
-                            fx[k] = fmaf(t, dx, fx[k]);
-                            fy[k] = fmaf(t, dy, fy[k]);
-                            fz[k] = fmaf(q.w, swz, fz[k]);
+                        }
+                    } else {  // some image straddles the cut: a per-pair test for those
+                        for (int jj = 0; jj < T; ++jj) {
+                            const float4 q = spb[jj];
+#pragma unroll
+                            for (int k = 0; k < IPT; k++) {
+                                const float dx = q.x - px[k], dy = q.y - py[k], dz = q.z - pz[k];
+                                const float rho2 = fmaf(dx, dx, dy * dy);
+                                float sw = 0.0f, swz = 0.0f;
+#pragma unroll
+                                for (int m = 0; m < NIMG; m++) {
+                                    const float dzm = dz + off[m];
+                                    const float ri = rsqrt_mufu(fmaf(dzm, dzm, rho2));
+                                    float ri3 = ri * ri * ri;
+                                    if (strad & (1u << m)) {  // block-uniform
+                                        bool in = fabsf(dzm) <= a.cutL;
+                                        if (fabsf(fabsf(dzm) - a.cutL) < a.cut_tol) {
+                                            float phz, plz;
+                                            frame_split(zi[k], lz[k], dOz, eOz, phz, plz);
+                                            in = cut_in_exact(q.z, sresb[jj].z, phz, plz, off[m], a.cutL);
+                                        }
+                                        ri3 = in ? ri3 : 0.0f;
+                                    }
+                                    sw += ri3;
+                                    swz = fmaf(ri3, dzm, swz);
+                                }
+                                const float t = q.w * sw;
+                                fx[k] = fmaf(t, dx, fx[k]);
+                                fy[k] = fmaf(t, dy, fy[k]);
+                                fz[k] = fmaf(q.w, swz, fz[k]);
+                            }
                         }
                     }
                 }
@@ -243,13 +288,8 @@ __global__ void __launch_bounds__(BLOCK, KIND == K_R3 && IPT == 1 ? 1024 / BLOCK
                                     // |dz + mL| <= (e - 0.4) L (StePS/src/forces.cc:1274), a hard
                                     // cut: within a hair of it, decide on a TwoSum-exact dz.
                                     bool in = fabsf(dzm) <= a.cutL;
-                                    if (!self && fabsf(fabsf(dzm) - a.cutL) < a.cut_tol) {
-                                        float e1, e2;
-                                        const float s1 = two_diff(q.z, phz[k], e1);
-                                        const float hh = two_diff(s1, -sh, e2);
-                                        const float tail = e2 + (e1 + (ql.z - plz[k]));
-                                        in = (fabsf(hh) - a.cutL) + copysignf(1.0f, hh) * tail <= 0.0f;
-                                    }
+                                    if (!self && fabsf(fabsf(dzm) - a.cutL) < a.cut_tol)
+                                        in = cut_in_exact(q.z, ql.z, phz[k], plz[k], sh, a.cutL);
                                     if (!in) w = 0.0f;
                                 }
                                 sw += w;

@@ -30,6 +30,17 @@ __device__ __forceinline__ int pmod(int i, int n)
     return r < 0 ? r + n : r;
 }
 
+// i mod n for i in [-2n, 3n), without a division; any other i (positions
+// outside the box, NaN) is clamped into [0, n) so the read stays in the table.
+__device__ __forceinline__ int wrap_index(int i, int n)
+{
+    i += i < 0 ? n : 0;
+    i += i < 0 ? n : 0;
+    i -= i >= n ? n : 0;
+    i -= i >= n ? n : 0;
+    return min(max(i, 0), n - 1);
+}
+
 template <int ORDER>
 __device__ __forceinline__ void weights(float t, float *w)
 {
@@ -127,10 +138,15 @@ __global__ void __launch_bounds__(BLOCK) k_pair_t3(MixedArgs a)
                               coarse_for_gap(dO[0], dO[1], dO[2], mI1, mJ1, g2, a.guard2);
             // Window strides are odd so that neighbouring cells fall in
             // different shared-memory banks; cells past wn[] are padding.
-            const int sy = ORDER != 0 ? (wn[2] | 1) : 0;
-            const int sx = ORDER != 0 ? ((wn[1] * sy) | 1) : 0;
-            const int ncell = ORDER != 0 ? wn[0] * sx : 0;
-            const bool use_win = ORDER != 0 && ncell <= a.wcap;
+            // Non-finite or out-of-box input can make wn[] anything: the
+            // window is used only when every extent is in [NT, wcap].
+            bool use_win = ORDER != 0;
+#pragma unroll
+            for (int ax3 = 0; ax3 < 3; ax3++) use_win = use_win && wn[ax3] >= NT && wn[ax3] <= a.wcap;
+            const int sy = use_win ? (wn[2] | 1) : 0;
+            const int sx = use_win ? ((wn[1] * sy) | 1) : 0;
+            use_win = use_win && (long long)wn[0] * sx <= (long long)a.wcap;
+            const int ncell = use_win ? wn[0] * sx : 0;
 
             if (J + 1 < J1) {
                 stage_tile<BLOCK, IPT>(a, J + 1, sp[buf ^ 1], se[buf ^ 1], sid[buf ^ 1], sres[buf ^ 1]);
@@ -211,9 +227,11 @@ __global__ void __launch_bounds__(BLOCK) k_pair_t3(MixedArgs a)
                             weights<ORDER>(ux - fxl, wx);
                             weights<ORDER>(uy - fyl, wy);
                             weights<ORDER>(uz - fzl, wz);
-                            bx = (int)fxl - OFF;
-                            by = (int)fyl - OFF;
-                            bz = (int)fzl - OFF;
+                            // The window covers every stencil of the tile pair; the
+                            // clamps only keep non-finite input inside it.
+                            bx = min(max((int)fxl - OFF, 0), wn[0] - NT);
+                            by = min(max((int)fyl - OFF, 0), wn[1] - NT);
+                            bz = min(max((int)fzl - OFF, 0), wn[2] - NT);
                             const float4 *base = win + (bx * sx + by * sy + bz);
 #pragma unroll(ORDER == 4 ? 1 : NT)
                             for (int aa = 0; aa < NT; aa++)
@@ -239,14 +257,24 @@ __global__ void __launch_bounds__(BLOCK) k_pair_t3(MixedArgs a)
                             bx = (int)fxl - OFF;
                             by = (int)fyl - OFF;
                             bz = (int)fzl - OFF;
+                            // Stencil indices wrapped once per axis: |d| < 3L/2,
+                            // so every index lies in [-2 ng, 3 ng).
+                            int gx[NT], gy[NT], gz[NT];
+#pragma unroll
+                            for (int t = 0; t < NT; t++) {
+                                gx[t] = wrap_index(bx + t, a.ng);
+                                gy[t] = wrap_index(by + t, a.ng);
+                                gz[t] = wrap_index(bz + t, a.ng);
+                            }
+#pragma unroll(ORDER == 4 ? 1 : NT)
                             for (int aa = 0; aa < NT; aa++) {
-                                const int gx = pmod(bx + aa, a.ng);
+#pragma unroll
                                 for (int bb = 0; bb < NT; bb++) {
-                                    const int gy = pmod(by + bb, a.ng);
+                                    const float4 *row = a.t3f + (gx[aa] * a.ng + gy[bb]) * a.ng;
                                     const float wxy = wx[aa] * wy[bb];
+#pragma unroll
                                     for (int cc = 0; cc < NT; cc++) {
-                                        const int gz = pmod(bz + cc, a.ng);
-                                        const float4 v = __ldg(a.t3f + ((size_t)gx * a.ng + gy) * a.ng + gz);
+                                        const float4 v = __ldg(row + gz[cc]);
                                         const float ww = wxy * wz[cc];
                                         Dx = fmaf(ww, v.x, Dx);
                                         Dy = fmaf(ww, v.y, Dy);
@@ -506,14 +534,11 @@ KernelFn pick_t3(int threads, int ipt)
 
 }  // namespace
 
-// Window capacity (cells) of the T^3 kernels' shared-memory table staging.
-constexpr int T3_WINDOW_CELLS = 2048;
-
 KernelFn t3_kernel(const KParams &kp, int threads, int ipt, size_t *dyn_smem)
 {
     *dyn_smem = 0;
     if (kp.is_periodic < 2) return pick_t3<0>(threads, ipt);
-    *dyn_smem = T3_WINDOW_CELLS * sizeof(float4);
+    *dyn_smem = (size_t)ctx().shape.t3_cells * sizeof(float4);
     return kp.order == 4 ? pick_t3<4>(threads, ipt) : pick_t3<2>(threads, ipt);
 }
 
@@ -537,7 +562,7 @@ void t3_args(MixedArgs &a, const KParams &kp, const Tables &tb, cudaStream_t st)
     a.ng = tb.t3_ng;
     a.ih = 0.0f;
     a.u0 = 0.0f;
-    a.wcap = T3_WINDOW_CELLS;
+    a.wcap = ctx().shape.t3_cells;
     if (kp.is_periodic >= 2) {
         a.t3f = t3_table_f32(tb, st);
         a.ih = (float)((double)tb.t3_ng / kp.L);
