@@ -44,6 +44,10 @@ UNIT = "pairs/s"
 # (index radius 3), k vectors |k| <= 5 (2 pi / L) (index radius 6).
 T3_NG = 63
 LOOPS = ["fp32", "fp32x2", "fp32x2 (768 threads/SM)", "fp32x2 (1024 threads/SM)"]
+# DRAM bytes (read + write) of one launch of the pair kernel, from a one-pass ncu
+# capture of dram__bytes_read.sum + dram__bytes_write.sum (profiles/launches_r3_n1048576.md):
+# N = 2^20 R^3, 256x1 packed at 768 threads/SM, 64 j chunks.
+NCU_TRAFFIC = {("cfg1", 1 << 20): 104.15e6 + 1.60e9}
 
 
 def parse():
@@ -185,16 +189,17 @@ def cpu_baseline(ps, p, sample: int, threads: int, table=None, ngrid=0, seconds:
                     order=p.ewald_order)
     lo = ps.n // 2
     probe = min(max(threads, 8), ps.n - lo)
-    while True:  # warm-up and calibration: grow the probe until it takes 0.25 s
+    port.forces(s, ps.x, lo, lo + probe - 1)  # warm-up: threads, pages
+    target = min(1.0, seconds / 4)
+    while True:  # calibration: grow the probe until it takes `target` seconds
         t0 = time.perf_counter()
         port.forces(s, ps.x, lo, lo + probe - 1)
         dt = time.perf_counter() - t0
-        if dt >= 0.25 or probe >= ps.n - lo:
+        if dt >= target or probe >= ps.n - lo:
             break
-        probe = min(4 * probe, ps.n - lo)
-    rate0 = probe * ps.n / max(dt, 1e-9)
+        probe = min(max(2 * probe, int(probe * target / max(dt, 1e-9))), ps.n - lo)
     if sample <= 0:
-        sample = int(rate0 * seconds / ps.n)
+        sample = int(probe * seconds / max(dt, 1e-9))
     sample = max(8, min(sample, ps.n - lo))
     hi = lo + sample - 1
     t0 = time.perf_counter()
@@ -323,7 +328,10 @@ def run_ours(args, ws, rank, local, dist):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(ps.x.nbytes),
                 "d2h_bytes_per_step": int(F_host.nbytes), "ms_per_step": e2e_t * 1e3},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": f32_peak / 1e12, "unit": "TFLOP/s",
-                     "frac": achieved / (f32_peak / 1e12), "traffic": None,
+                     "frac": achieved / (f32_peak / 1e12),
+                     "traffic": NCU_TRAFFIC.get((args.workload, n)),
+                     "traffic_note": "DRAM bytes of one pair-kernel launch from an ncu capture (None: not captured "
+                                     "for this size); compute-bound, under 0.1 % of HBM bandwidth",
                      "peak_kind": "FP32 FMA issue peak measured in this process (dependent-FMA-chain kernel)",
                      "nominal_peak_at_max_clock": nominal, "frac_of_nominal": achieved / nominal,
                      "flops_per_pair": flops, "kernel_ms": kern_ms},

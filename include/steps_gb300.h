@@ -195,10 +195,9 @@ int steps_gpu_set_kernel_variant(int variant);
 
 /* T^3 mixed precision: capacity, in table cells (16 bytes each), of the
  * shared-memory window of the Ewald table that each block stages per tile
- * pair. Tile pairs whose window does not fit read the table through L1/L2.
- * 0 disables the window. Default 1024; at most STEPS_T3_WINDOW_MAX.
- * steps_gpu_autotune searches 0, 1024 and 2048 for trilinear tables and
- * uses 2048 for tricubic ones. */
+ * pair. Without a window (0, the default), or when a tile pair's window does
+ * not fit, pairs read an FP32 copy of the table with a periodic halo through
+ * L1/L2. At most STEPS_T3_WINDOW_MAX. */
 #define STEPS_T3_WINDOW_MAX 12288
 int steps_gpu_set_t3_window(int cells);
 
@@ -209,9 +208,9 @@ int steps_gpu_set_t3_window(int cells);
 int steps_gpu_set_precision_guard(double ratio);
 
 /* Times every supported mixed-precision shape on the resident particles for
- * the given topology -- for R^3 with each pair-loop variant, for trilinear
- * T^3 with each table-window size -- and keeps the fastest; writes threads,
- * ipt, variant to out[3]. One evaluation per candidate. */
+ * the given topology -- for R^3 with each pair-loop variant -- and keeps the
+ * fastest; writes threads, ipt, variant to out[3]. One evaluation per
+ * candidate. */
 int steps_gpu_autotune(const steps_params *p, int id_min, int id_max, int *out);
 
 /* Number of kernels this library has launched since init. */

@@ -428,30 +428,24 @@ int steps_gpu_autotune(const steps_params *p, int id_min, int id_max, int *out)
         float best = 1e30f;
         Shape bestS = keep;
         KParams kp = derive_params(p);
-        // R^3: scalar and packed pair loops; T^3 trilinear: table window sizes
-        // (tricubic keeps 2048 cells, nearest-image T^3 has no table).
+        // R^3: the scalar and packed pair loops as well.
         const int nvar = kp.topology == STEPS_R3 ? 4 : 1;
-        const bool t3w = kp.topology == STEPS_T3 && kp.is_periodic >= 2 && kp.order == 2;
-        const int windows[] = {1024, 0, 2048};
-        const int nwin = t3w ? 3 : 1;
         compute_forces(p, STEPS_MIXED, id_min, id_max, false);  // orders the particles, loads modules
         for (int v = 0; v < nvar; v++)
-            for (auto &s : shapes)
-                for (int w = 0; w < nwin; w++) {
-                    if (!shape_supported_for(kp, s[0], s[1])) continue;
-                    if (v >= 1 && !r3x2_kernel(s[0], s[1], false, r3x2_occ(v))) continue;
-                    c.shape.threads = s[0];
-                    c.shape.ipt = s[1];
-                    c.shape.jsplit = 0;
-                    c.shape.variant = v;
-                    c.shape.t3_cells = kp.topology != STEPS_T3 ? keep.t3_cells : t3w ? windows[w] : 2048;
-                    // one timed evaluation per candidate: the phase events bracket the pair kernel only
-                    compute_forces(p, STEPS_MIXED, id_min, id_max, true);
-                    STEPS_CUDA(cudaEventSynchronize(c.phase[2]));
-                    float ms = 0;
-                    STEPS_CUDA(cudaEventElapsedTime(&ms, c.phase[1], c.phase[2]));
-                    if (ms < best) { best = ms; bestS = c.shape; }
-                }
+            for (auto &s : shapes) {
+                if (!shape_supported_for(kp, s[0], s[1])) continue;
+                if (v >= 1 && !r3x2_kernel(s[0], s[1], false, r3x2_occ(v))) continue;
+                c.shape.threads = s[0];
+                c.shape.ipt = s[1];
+                c.shape.jsplit = 0;
+                c.shape.variant = v;
+                // one timed evaluation per candidate: the phase events bracket the pair kernel only
+                compute_forces(p, STEPS_MIXED, id_min, id_max, true);
+                STEPS_CUDA(cudaEventSynchronize(c.phase[2]));
+                float ms = 0;
+                STEPS_CUDA(cudaEventElapsedTime(&ms, c.phase[1], c.phase[2]));
+                if (ms < best) { best = ms; bestS = c.shape; }
+            }
         c.shape = bestS;
         c.shape_fixed = true;
         if (out) { out[0] = bestS.threads; out[1] = bestS.ipt; out[2] = bestS.variant; }

@@ -43,6 +43,7 @@ struct Batch {
     DevBuf tslot;                 // int2 per tile: first partial slot, number of slots
     DevBuf part, counter, err;
     int T = 0, ntiles = 0, nitems = 0, threads = 0, ipt = 0, grid = 0;
+    long long graph_kernels = 0;
     bool tuned = false;
     cudaGraphExec_t exec = nullptr;
     int graph_steps = -1;
@@ -249,6 +250,22 @@ void plain_steps(Batch &b, const KParams &kp, int precision, int nsteps, double 
     }
 }
 
+// Kernel nodes of a captured graph (what one launch of it runs).
+long long count_kernel_nodes(cudaGraph_t g)
+{
+    size_t n = 0;
+    STEPS_CUDA(cudaGraphGetNodes(g, nullptr, &n));
+    std::vector<cudaGraphNode_t> nodes(n);
+    if (n) STEPS_CUDA(cudaGraphGetNodes(g, nodes.data(), &n));
+    long long k = 0;
+    for (size_t i = 0; i < n; i++) {
+        cudaGraphNodeType t;
+        STEPS_CUDA(cudaGraphNodeGetType(nodes[i], &t));
+        k += t == cudaGraphNodeTypeKernel;
+    }
+    return k;
+}
+
 void release_graph(Batch &b)
 {
     if (b.exec) cudaGraphExecDestroy(b.exec);
@@ -409,6 +426,7 @@ int steps_gpu_batch_run(const steps_params *p, int precision, int nsteps, double
                     throw;
                 }
                 STEPS_CUDA(cudaStreamEndCapture(c.stream, &g));
+                b.graph_kernels = count_kernel_nodes(g);
                 cudaError_t e = cudaGraphInstantiate(&b.exec, g, 0);
                 cudaGraphDestroy(g);
                 STEPS_CUDA(e);
@@ -416,7 +434,7 @@ int steps_gpu_batch_run(const steps_params *p, int precision, int nsteps, double
                 b.graph_h = a.h;
             }
             STEPS_CUDA(cudaGraphLaunch(b.exec, c.stream));
-            c.launches += 1;
+            c.launches += b.graph_kernels;  // the kernels the graph runs
             STEPS_CUDA(cudaStreamSynchronize(c.stream));
         },
         &args);

@@ -87,7 +87,7 @@ struct Shape {
     int jsplit = 0;
     int variant = 0;  // R^3: 0 scalar FP32 pair loop; 1, 2, 3 packed FP32x2 (0, 768, 1024 threads/SM asked)
     float guard = 30.0f;  // tile-pair scale / gap above which the double-float path runs
-    int t3_cells = 1024;  // T^3: shared-memory table window capacity in cells (0 = table from L2)
+    int t3_cells = 0;  // T^3: shared-memory table window capacity in cells (0 = haloed table via L1/L2)
 };
 
 // ------------------------------------------------------------- utilities --

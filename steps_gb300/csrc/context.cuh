@@ -32,7 +32,7 @@ struct Ctx {
     DevBuf t3;
     int t3_ng = 0;
     long long t3_version = 0;  // bumped whenever the table changes
-    DevBuf t3f;                // FP32 float4-per-cell copy for the mixed kernels
+    DevBuf t3f;                // FP32 float4-per-cell haloed copy for the mixed kernels
     long long t3f_version = -1;
     DevBuf s1r2;
     int nrho = 0, nz = 0;

@@ -41,6 +41,7 @@ struct MixedArgs {
     int ng;
     float ih, u0;       // continuous cell index u(d) = d * ih + u0, ih = ng / L, u0 = ng/2 - 1/2
     int wcap;           // cells of the shared-memory table window
+    int halo, ext;      // the FP32 copy is haloed: ext^3 cells, ext = ng + 2 halo
     // S1xR2 (rho, z) correction table (FP32 float2 copy) and its geometry
     const float2 *s1tab;
     int nrho, nz;
@@ -155,6 +156,96 @@ __device__ __forceinline__ bool cut_in_exact(float qz, float qlz, float phz, flo
 
 // Lower bound of |d| over the separations of two boxes along one axis.
 __device__ __forceinline__ float axis_gap(float dO, float hI, float hJ) { return fmaxf(fabsf(dO) - hI - hJ, 0.0f); }
+
+// Box of the i particles of this warp (FP32 offsets from I's centre, IPT per
+// lane): centre c and half extents h, widened by 1e-6 relative so that it also
+// holds the exact positions (offset + residual) whatever the FP32 rounding.
+template <int IPT>
+__device__ __forceinline__ void warp_box(const float *xi, const float *yi, const float *zi, float4 &c, float4 &h)
+{
+    float lo[3] = {xi[0], yi[0], zi[0]}, hi[3] = {xi[0], yi[0], zi[0]};
+#pragma unroll
+    for (int k = 1; k < IPT; k++) {
+        lo[0] = fminf(lo[0], xi[k]); hi[0] = fmaxf(hi[0], xi[k]);
+        lo[1] = fminf(lo[1], yi[k]); hi[1] = fmaxf(hi[1], yi[k]);
+        lo[2] = fminf(lo[2], zi[k]); hi[2] = fmaxf(hi[2], zi[k]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            lo[d] = fminf(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
+            hi[d] = fmaxf(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
+        }
+    float cc[3], hh[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        cc[d] = 0.5f * (lo[d] + hi[d]);
+        hh[d] = fmaxf(hi[d] - cc[d], cc[d] - lo[d]) * 1.000001f + 1e-6f * fabsf(cc[d]);
+    }
+    c = make_float4(cc[0], cc[1], cc[2], 0.0f);
+    h = make_float4(hh[0], hh[1], hh[2], 0.0f);
+}
+
+// Whether a warp with i box (c, h) in I's frame needs the near-field path
+// against tile J (offset d_O from I's centre, half extents hJ): some pair may
+// be closer than bmax = eps_max(I) + eps_max(J), or the FP32 scale of its
+// offsets is coarse for its gap (coarse_for_gap). The box offset carries the
+// FP32 rounding of d_O - c, covered by 1e-6 of |d_O| + |c|.
+__device__ __forceinline__ bool warp_full(float dOx, float dOy, float dOz, float4 c, float4 h, float4 hJ, float bmax,
+                                          float guard2)
+{
+    const float dx = dOx - c.x, dy = dOy - c.y, dz = dOz - c.z;
+    const float4 hw = make_float4(h.x + 1e-6f * (fabsf(dOx) + fabsf(c.x)), h.y + 1e-6f * (fabsf(dOy) + fabsf(c.y)),
+                                  h.z + 1e-6f * (fabsf(dOz) + fabsf(c.z)), 0.0f);
+    const float gx = axis_gap(dx, hw.x, hJ.x), gy = axis_gap(dy, hw.y, hJ.y), gz = axis_gap(dz, hw.z, hJ.z);
+    const float g2 = gx * gx + gy * gy + gz * gz;
+    return g2 <= bmax * bmax * 1.0001f + 1e-30f || coarse_for_gap(dx, dy, dz, hw, hJ, g2, guard2);
+}
+
+// Packed FP32 pairs (PTX .f32x2, sm_100+).
+typedef unsigned long long f2;  // two FP32 values in a 64-bit register pair; low half = first
+
+__device__ __forceinline__ f2 f2_bcast(float v)
+{
+    f2 r;
+    asm("mov.b64 %0, {%1, %1};" : "=l"(r) : "f"(v));
+    return r;
+}
+__device__ __forceinline__ f2 f2_pack(float lo, float hi)
+{
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void f2_unpack(f2 v, float &lo, float &hi)
+{
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f2 f2_sub(f2 a, f2 b)
+{
+    f2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 f2_add(f2 a, f2 b)
+{
+    f2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 f2_mul(f2 a, f2 b)
+{
+    f2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 f2_fma(f2 a, f2 b, f2 c)
+{
+    f2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
 
 using KernelFn = void (*)(MixedArgs);
 

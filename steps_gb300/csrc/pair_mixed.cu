@@ -76,6 +76,9 @@ __global__ void __launch_bounds__(BLOCK, KIND == K_R3 && IPT == 1 ? 1024 / BLOCK
             ax[k] = ay[k] = az[k] = 0.0;
         }
 
+        float4 wc = make_float4(0.f, 0.f, 0.f, 0.f), wh = wc;  // this warp's i box in I's frame (R^3)
+        if (KIND == K_R3) warp_box<IPT>(xi, yi, zi, wc, wh);
+
         if (J0 < J1) stage_tile<BLOCK, IPT>(a, J0, sp[0], se[0], sid[0], sres[0]);
         for (int J = J0; J < J1; ++J) {
             const int buf = (J - J0) & 1;
@@ -102,10 +105,8 @@ __global__ void __launch_bounds__(BLOCK, KIND == K_R3 && IPT == 1 ? 1024 / BLOCK
             bool full;  // near-field tile pair: softening and every test per pair
             float off[NIMG];
             unsigned strad = 0u;  // S1 images straddling the cut over this tile pair
-            if (KIND == K_R3) {
-                const float gz = axis_gap(dOz, mI1.z, mJ1.z);
-                const float g2 = gx * gx + gy * gy + gz * gz;
-                full = g2 <= bmax2 || coarse_for_gap(dOx, dOy, dOz, mI1, mJ1, g2, a.guard2);
+            if (KIND == K_R3) {  // per warp: warps away from a near J keep the far loop
+                full = warp_full(dOx, dOy, dOz, wc, wh, mJ1, bmax, a.guard2);
             } else if (KIND == K_S1_IMG) {
                 // Range of dz over the tile pair, then per image m: entirely
                 // inside the cut (offset m L), entirely outside (offset 1e18,
@@ -472,6 +473,7 @@ void forces_mixed(const KParams &kp, const Tables &tb, const double *x, const do
     a.ng = 0;
     a.ih = a.u0 = 0.0f;
     a.wcap = 0;
+    a.halo = a.ext = 0;
     a.s1tab = nullptr;
     a.nrho = a.nz = 0;
     a.irho = a.iz = a.rho_max = 0.0f;

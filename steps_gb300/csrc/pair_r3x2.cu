@@ -22,43 +22,6 @@ namespace {
 
 using namespace mixed;
 
-typedef unsigned long long f2;  // two FP32 values in a 64-bit register pair; low half = first
-
-__device__ __forceinline__ f2 f2_bcast(float v)
-{
-    f2 r;
-    asm("mov.b64 %0, {%1, %1};" : "=l"(r) : "f"(v));
-    return r;
-}
-__device__ __forceinline__ f2 f2_pack(float lo, float hi)
-{
-    f2 r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-    return r;
-}
-__device__ __forceinline__ void f2_unpack(f2 v, float &lo, float &hi)
-{
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
-}
-__device__ __forceinline__ f2 f2_sub(f2 a, f2 b)
-{
-    f2 r;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f2 f2_mul(f2 a, f2 b)
-{
-    f2 r;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f2 f2_fma(f2 a, f2 b, f2 c)
-{
-    f2 r;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
-    return r;
-}
-
 template <int BLOCK, int IPT>
 __device__ __forceinline__ void stage_soa(const MixedArgs &a, int J, float *sx, float *se, uint32_t *sid, float4 *sres)
 {
@@ -131,6 +94,9 @@ __device__ __forceinline__ void r3x2_body(const MixedArgs &a)
             ax[k] = ay[k] = az[k] = 0.0;
         }
 
+        float4 wc, wh;  // this warp's i box in I's frame
+        warp_box<IPT>(xi, yi, zi, wc, wh);
+
         if (J0 < J1) stage_soa<BLOCK, IPT>(a, J0, sx[0], se[0], sid[0], sres[0]);
         for (int J = J0; J < J1; ++J) {
             const int buf = (J - J0) & 1;
@@ -147,11 +113,9 @@ __device__ __forceinline__ void r3x2_body(const MixedArgs &a)
             float eOx, eOy, eOz;
             const float dOx = two_diff(mJ0.x, mI0.x, eOx), dOy = two_diff(mJ0.y, mI0.y, eOy),
                         dOz = two_diff(mJ0.z, mI0.z, eOz);
-            const float bmax = mI0.w + mJ0.w;
-            const float gx = axis_gap(dOx, mI1.x, mJ1.x), gy = axis_gap(dOy, mI1.y, mJ1.y),
-                        gz = axis_gap(dOz, mI1.z, mJ1.z);
-            const float g2 = gx * gx + gy * gy + gz * gz;
-            const bool full = g2 <= bmax * bmax * 1.0001f + 1e-30f || coarse_for_gap(dOx, dOy, dOz, mI1, mJ1, g2, a.guard2);
+            // Near field / coarse FP32 scale, decided per warp (warp-uniform
+            // branch): in a near tile pair, warps away from J keep the far loop.
+            const bool full = warp_full(dOx, dOy, dOz, wc, wh, mJ1, mI0.w + mJ0.w, a.guard2);
             const float *X = sx[buf];
             const float *Y = X + T;
             const float *Z = X + 2 * T;

@@ -56,6 +56,28 @@ __device__ __forceinline__ void weights(float t, float *w)
     }
 }
 
+// Sum of the NT^3 stencil taps fetch(a, b, c) weighted by wx[a] wy[b] wz[c].
+template <int ORDER, class Fetch>
+__device__ __forceinline__ void stencil(const float *wx, const float *wy, const float *wz, Fetch fetch, float &Dx,
+                                        float &Dy, float &Dz)
+{
+    constexpr int NT = ORDER;
+#pragma unroll(ORDER == 4 ? 1 : NT)
+    for (int aa = 0; aa < NT; aa++)
+#pragma unroll
+        for (int bb = 0; bb < NT; bb++) {
+            const float wxy = wx[aa] * wy[bb];
+#pragma unroll
+            for (int cc = 0; cc < NT; cc++) {
+                const float4 v = fetch(aa, bb, cc);
+                const float ww = wxy * wz[cc];
+                Dx = fmaf(ww, v.x, Dx);
+                Dy = fmaf(ww, v.y, Dy);
+                Dz = fmaf(ww, v.z, Dz);
+            }
+        }
+}
+
 // ORDER 0: IS_PERIODIC == 1, nearest image only (no table).
 template <int BLOCK, int IPT, int ORDER>
 __global__ void __launch_bounds__(BLOCK) k_pair_t3(MixedArgs a)
@@ -147,6 +169,12 @@ __global__ void __launch_bounds__(BLOCK) k_pair_t3(MixedArgs a)
             const int sx = use_win ? ((wn[1] * sy) | 1) : 0;
             use_win = use_win && (long long)wn[0] * sx <= (long long)a.wcap;
             const int ncell = use_win ? wn[0] * sx : 0;
+            // Otherwise the stencils of this tile pair lie inside the table's
+            // periodic halo (no per-pair wrap), or take the wrapped lookup.
+            bool halo = ORDER != 0 && !use_win;
+#pragma unroll
+            for (int ax3 = 0; ax3 < 3; ax3++)
+                halo = halo && w0[ax3] >= -a.halo && w0[ax3] + wn[ax3] <= a.ng + a.halo;
 
             if (J + 1 < J1) {
                 stage_tile<BLOCK, IPT>(a, J + 1, sp[buf ^ 1], se[buf ^ 1], sid[buf ^ 1], sres[buf ^ 1]);
@@ -161,7 +189,7 @@ __global__ void __launch_bounds__(BLOCK) k_pair_t3(MixedArgs a)
                     const int cy = rem / sy;
                     const int cz = rem - cy * sy;
                     const int gx = pmod(w0[0] + cx, a.ng), gy = pmod(w0[1] + cy, a.ng), gz = pmod(w0[2] + cz, a.ng);
-                    win[cidx] = __ldg(a.t3f + ((size_t)gx * a.ng + gy) * a.ng + gz);
+                    win[cidx] = __ldg(a.t3f + ((gx + a.halo) * a.ext + gy + a.halo) * a.ext + gz + a.halo);
                 }
             }
             __syncthreads();
@@ -220,7 +248,7 @@ __global__ void __launch_bounds__(BLOCK) k_pair_t3(MixedArgs a)
                     if (ORDER != 0) {
                         float wx[4], wy[4], wz[4];
                         int bx, by, bz;
-                        if (use_win) {
+                        if (use_win) {  // shared-memory window, window-local cell index
                             const float ux = fmaf(dx, a.ih, uc[0]), uy = fmaf(dy, a.ih, uc[1]),
                                         uz = fmaf(dz, a.ih, uc[2]);
                             const float fxl = floorf(ux), fyl = floorf(uy), fzl = floorf(uz);
@@ -233,21 +261,24 @@ __global__ void __launch_bounds__(BLOCK) k_pair_t3(MixedArgs a)
                             by = min(max((int)fyl - OFF, 0), wn[1] - NT);
                             bz = min(max((int)fzl - OFF, 0), wn[2] - NT);
                             const float4 *base = win + (bx * sx + by * sy + bz);
-#pragma unroll(ORDER == 4 ? 1 : NT)
-                            for (int aa = 0; aa < NT; aa++)
-#pragma unroll
-                                for (int bb = 0; bb < NT; bb++) {
-                                    const float wxy = wx[aa] * wy[bb];
-#pragma unroll
-                                    for (int cc = 0; cc < NT; cc++) {
-                                        const float4 v = base[aa * sx + bb * sy + cc];
-                                        const float ww = wxy * wz[cc];
-                                        Dx = fmaf(ww, v.x, Dx);
-                                        Dy = fmaf(ww, v.y, Dy);
-                                        Dz = fmaf(ww, v.z, Dz);
-                                    }
-                                }
-                        } else {
+                            stencil<ORDER>(wx, wy, wz, [&](int aa, int bb, int cc) { return base[aa * sx + bb * sy + cc]; },
+                                           Dx, Dy, Dz);
+                        } else if (halo) {  // haloed table in L1/L2, no wrap
+                            const float uh = a.u0 + (float)a.halo;
+                            const float ux = fmaf(dx, a.ih, uh), uy = fmaf(dy, a.ih, uh), uz = fmaf(dz, a.ih, uh);
+                            const float fxl = floorf(ux), fyl = floorf(uy), fzl = floorf(uz);
+                            weights<ORDER>(ux - fxl, wx);
+                            weights<ORDER>(uy - fyl, wy);
+                            weights<ORDER>(uz - fzl, wz);
+                            const int E = a.ext;
+                            bx = min(max((int)fxl - OFF, 0), E - NT);
+                            by = min(max((int)fyl - OFF, 0), E - NT);
+                            bz = min(max((int)fzl - OFF, 0), E - NT);
+                            const float4 *base = a.t3f + ((bx * E + by) * E + bz);
+                            stencil<ORDER>(wx, wy, wz,
+                                           [&](int aa, int bb, int cc) { return __ldg(base + (aa * E + bb) * E + cc); },
+                                           Dx, Dy, Dz);
+                        } else {  // wrapped lookup (tile pairs wider than the halo)
                             const float ux = fmaf(dx, a.ih, a.u0), uy = fmaf(dy, a.ih, a.u0),
                                         uz = fmaf(dz, a.ih, a.u0);
                             const float fxl = floorf(ux), fyl = floorf(uy), fzl = floorf(uz);
@@ -262,26 +293,15 @@ __global__ void __launch_bounds__(BLOCK) k_pair_t3(MixedArgs a)
                             int gx[NT], gy[NT], gz[NT];
 #pragma unroll
                             for (int t = 0; t < NT; t++) {
-                                gx[t] = wrap_index(bx + t, a.ng);
-                                gy[t] = wrap_index(by + t, a.ng);
-                                gz[t] = wrap_index(bz + t, a.ng);
+                                gx[t] = wrap_index(bx + t, a.ng) + a.halo;
+                                gy[t] = wrap_index(by + t, a.ng) + a.halo;
+                                gz[t] = wrap_index(bz + t, a.ng) + a.halo;
                             }
-#pragma unroll(ORDER == 4 ? 1 : NT)
-                            for (int aa = 0; aa < NT; aa++) {
-#pragma unroll
-                                for (int bb = 0; bb < NT; bb++) {
-                                    const float4 *row = a.t3f + (gx[aa] * a.ng + gy[bb]) * a.ng;
-                                    const float wxy = wx[aa] * wy[bb];
-#pragma unroll
-                                    for (int cc = 0; cc < NT; cc++) {
-                                        const float4 v = __ldg(row + gz[cc]);
-                                        const float ww = wxy * wz[cc];
-                                        Dx = fmaf(ww, v.x, Dx);
-                                        Dy = fmaf(ww, v.y, Dy);
-                                        Dz = fmaf(ww, v.z, Dz);
-                                    }
-                                }
-                            }
+                            stencil<ORDER>(wx, wy, wz,
+                                           [&](int aa, int bb, int cc) {
+                                               return __ldg(a.t3f + (gx[aa] * a.ext + gy[bb]) * a.ext + gz[cc]);
+                                           },
+                                           Dx, Dy, Dz);
                         }
                     }
                     fx[k] = fmaf(q.w, fmaf(w, nx, -Dx), fx[k]);
@@ -516,10 +536,18 @@ KernelFn pick_s1tab(int threads, int ipt)
     return nullptr;
 }
 
-__global__ void k_table_f32(const double *__restrict__ t, size_t ncell, float4 *__restrict__ out)
+// FP32 copy of the ng^3 table with a periodic halo of `halo` cells on every
+// side: cell (i, j, k) of the ext^3 copy, ext = ng + 2 halo, is table cell
+// ((i - halo) mod ng, (j - halo) mod ng, (k - halo) mod ng).
+__global__ void k_table_f32(const double *__restrict__ t, int ng, int halo, float4 *__restrict__ out)
 {
+    const int ext = ng + 2 * halo;
+    const size_t ncell = (size_t)ext * ext * ext;
     size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c < ncell) out[c] = make_float4((float)t[3 * c], (float)t[3 * c + 1], (float)t[3 * c + 2], 0.0f);
+    if (c >= ncell) return;
+    const int k = (int)(c % ext), j = (int)((c / ext) % ext), i = (int)(c / ((size_t)ext * ext));
+    const size_t s = ((size_t)pmod(i - halo, ng) * ng + pmod(j - halo, ng)) * ng + pmod(k - halo, ng);
+    out[c] = make_float4((float)t[3 * s], (float)t[3 * s + 1], (float)t[3 * s + 2], 0.0f);
 }
 
 template <int ORDER>
@@ -542,14 +570,19 @@ KernelFn t3_kernel(const KParams &kp, int threads, int ipt, size_t *dyn_smem)
     return kp.order == 4 ? pick_t3<4>(threads, ipt) : pick_t3<2>(threads, ipt);
 }
 
-// FP32 float4 copy of the FP64 table, rebuilt whenever the table changes.
+// Halo of the FP32 table copy: tile pairs whose stencils stay within it need
+// no per-pair index wrap.
+constexpr int T3_HALO = 16;
+
+// FP32 float4 haloed copy of the FP64 table, rebuilt whenever the table changes.
 const float4 *t3_table_f32(const Tables &tb, cudaStream_t st)
 {
     Ctx &c = ctx();
-    size_t ncell = (size_t)tb.t3_ng * tb.t3_ng * tb.t3_ng;
+    const size_t ext = (size_t)tb.t3_ng + 2 * T3_HALO;
+    const size_t ncell = ext * ext * ext;
     if (c.t3f_version != c.t3_version || !c.t3f.p) {
         float4 *o = c.t3f.ensure<float4>(ncell);
-        k_table_f32<<<(unsigned)((ncell + 255) / 256), 256, 0, st>>>(tb.t3, ncell, o);
+        k_table_f32<<<(unsigned)((ncell + 255) / 256), 256, 0, st>>>(tb.t3, tb.t3_ng, T3_HALO, o);
         note_launch("k_table_f32");
         c.t3f_version = c.t3_version;
     }
@@ -563,6 +596,8 @@ void t3_args(MixedArgs &a, const KParams &kp, const Tables &tb, cudaStream_t st)
     a.ih = 0.0f;
     a.u0 = 0.0f;
     a.wcap = ctx().shape.t3_cells;
+    a.halo = T3_HALO;
+    a.ext = tb.t3_ng + 2 * T3_HALO;
     if (kp.is_periodic >= 2) {
         a.t3f = t3_table_f32(tb, st);
         a.ih = (float)((double)tb.t3_ng / kp.L);

@@ -77,6 +77,7 @@ namespace {
 struct LegacyState {
     bool ready = false;
     int precision = STEPS_MIXED;
+    bool tune = true;  // autotune the mixed kernel after the first mixed force call
     std::vector<double> m, eps;  // what the device holds
     const void *table_ptr = nullptr;
     long long table_size = -1;
@@ -99,6 +100,8 @@ bool ensure_context()
     const char *dev = getenv("STEPS_GB300_DEVICE");
     const char *prec = getenv("STEPS_GB300_PRECISION");
     if (prec && strcmp(prec, "fp64") == 0) S.precision = STEPS_FP64;
+    const char *tune = getenv("STEPS_GB300_AUTOTUNE");
+    if (tune && strcmp(tune, "0") == 0) S.tune = false;
     if (n_GPU > 1 && rank == 0)
         fprintf(stderr, "steps_gb300: using one GPU per rank (n_GPU = %i requested)\n", n_GPU);
     if (steps_gpu_init(dev ? atoi(dev) : 0) != STEPS_OK) {
@@ -164,6 +167,13 @@ void run(const steps_params &p, REAL *x, REAL *F, int ID_min, int ID_max)
     if (steps_gpu_forces(&p, S.precision, xd, Fd, ID_min, ID_max) != STEPS_OK) {
         report("force evaluation");
         return;
+    }
+    if (S.tune && S.precision == STEPS_MIXED) {
+        // Once per run, on the positions just uploaded: time every kernel shape
+        // and keep the fastest for the following steps.
+        S.tune = false;
+        int shape[3];
+        if (steps_gpu_autotune(&p, ID_min, ID_max, shape) != STEPS_OK) report("autotune");
     }
 #ifdef USE_SINGLE_PRECISION
     for (size_t i = 0; i < 3 * (size_t)ni; i++) F[i] = (REAL)Fd[i];

@@ -21,6 +21,16 @@ FLAGS = {"r3": [], "t3": ["-DPERIODIC", "-DEWALD_INTERPOLATION_ORDER=4"],
 _dp = C.POINTER(C.c_double)
 
 
+@pytest.fixture(autouse=True)
+def default_shape(engine):
+    """The shim autotunes the library's kernel shape after its first mixed
+    call; later tests expect the defaults back."""
+    yield
+    engine.set_tuning(128, 2, 0)
+    engine.set_variant(0)
+    engine.set_t3_window(0)
+
+
 def harness(tmp_path_factory, variant):
     d = tmp_path_factory.mktemp("legacy_" + variant)
     out = str(d / f"libharness_{variant}.so")
@@ -60,7 +70,9 @@ def test_forces_r3(tmp_path_factory, engine):
     rc, F = run(h, g["x"], 0, lo, hi)
     assert rc == 0 and rel_err(F, g["F_sub"]).max() < 1e-12
     h.h_precision(S.MIXED)
-    rc, F = run(h, g["x"], 2048)
+    rc, F = run(h, g["x"], 2048)  # default shape, then the shim autotunes once
+    assert rc == 0 and err_stats(F, g["F"])["p99"] < 1e-5
+    rc, F = run(h, g["x"], 2048)  # the tuned shape
     assert rc == 0 and err_stats(F, g["F"])["p99"] < 1e-5
     # a bad i range sets ForceError instead of aborting
     rc, F = run(h, g["x"], 0, 10, 5000)

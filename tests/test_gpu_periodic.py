@@ -172,11 +172,18 @@ def test_t3_mixed_shapes_and_workload_table(engine, port, order):
                     order=order)
     Fo = port.forces(s, ps.x, 0, 255)
     assert rel_err(F64[:256], Fo).max() < FP64_TOL
-    for threads, ipt in ((64, 1), (64, 2), (128, 1), (128, 2), (256, 1)):
-        engine.set_tuning(threads, ipt, 0)
-        st = err_stats(engine.forces(ps.x, p, S.MIXED), F64)
-        assert st["p99"] < MIXED_P99, (threads, ipt, st)
-    engine.set_tuning(128, 2, 0)
+    try:
+        # table reads: haloed copy / wrapped (tile pairs wider than the halo) /
+        # shared-memory windows of two capacities
+        for cells in (0, 1024, 4096):
+            engine.set_t3_window(cells)
+            for threads, ipt in ((64, 1), (64, 2), (128, 1), (128, 2), (256, 1)):
+                engine.set_tuning(threads, ipt, 0)
+                st = err_stats(engine.forces(ps.x, p, S.MIXED), F64)
+                assert st["p99"] < MIXED_P99, (cells, threads, ipt, st)
+    finally:
+        engine.set_tuning(128, 2, 0)
+        engine.set_t3_window(0)
 
 
 def half_box_pairs(x, L, axes, seed, npairs):
