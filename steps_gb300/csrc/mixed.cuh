@@ -228,12 +228,6 @@ __device__ __forceinline__ f2 f2_sub(f2 a, f2 b)
     asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
     return r;
 }
-__device__ __forceinline__ f2 f2_add(f2 a, f2 b)
-{
-    f2 r;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
 __device__ __forceinline__ f2 f2_mul(f2 a, f2 b)
 {
     f2 r;

@@ -7,6 +7,7 @@ pin: tests/test_golden.py checks the plain-C oracle against them on any
 machine, and the GPU tests check the CUDA kernels against them.
 
 Run from the repository root:  python tests/golden/make_golden.py
+(``... make_golden.py fp32`` regenerates only the single-precision floor).
 """
 from __future__ import annotations
 
@@ -152,5 +153,39 @@ def main():
     save("softening", r=rs, w_beta1=w, w_beta037=w2)
 
 
+def fp32_floor():
+    """The reference's own single-precision build (USE_SINGLE_PRECISION) on the
+    same inputs as its FP64 build: the error floor of the reference's FP32 path
+    that the mixed kernels are compared with."""
+    # R^3: the N = 32,768 compactified workload (regenerated from its seed on
+    # any machine), i range [16128, 16640) against all j.
+    ps = W.r3_compactified(32768, 480.0, seed=0)
+    lo, hi = 16128, 16639
+    out = {}
+    for var in ("r3", "r3sp"):
+        ref = O.Ref(var)
+        ref.set_particles(ps.x, ps.m, ps.eps)
+        ref.set_params()
+        out[var] = ref.forces(lo, hi)
+    # T^3 trilinear and the S1xR2 image sum on the golden inputs.
+    g = np.load(os.path.join(HERE, "t3_o2.npz"))
+    ref = O.Ref("t3o2sp")
+    ref.set_particles(g["x"], g["m"], g["eps"])
+    ref.set_t3_table(g["table"], int(g["ngrid"]))
+    ref.set_params(is_periodic=2, L=float(g["L"]), rsim=float(g["L"]) / 2)
+    t3sp = ref.forces()
+    g = np.load(os.path.join(HERE, "s1r2_images.npz"))
+    ref = O.Ref("s1nlsp")
+    ref.set_particles(g["x"], g["m"], g["eps"])
+    ref.set_params(is_periodic=2, L=float(g["L"]), rsim=float(g["rsim"]))
+    s1sp = ref.forces()
+    save("ref_fp32", r3_n=np.array(32768), r3_rmax=np.array(480.0), r3_seed=np.array(0), r3_sub=np.array([lo, hi]),
+         r3_F64=out["r3"], r3_F32=out["r3sp"], t3o2_F32=t3sp, s1r2_is2_F32=s1sp)
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["fp32"]:
+        fp32_floor()
+    else:
+        main()
+        fp32_floor()

@@ -117,15 +117,18 @@ def test_shapes_agree(engine, port):
 
 
 def test_packed_fp32x2_variant(engine, port):
-    """The packed FP32x2 pair loop agrees with the reference like the scalar one."""
+    """The packed FP32x2 pair loop agrees with the reference like the scalar one,
+    at each register budget (variants 1-3)."""
     g = golden("r3_n2048")
     engine.set_particles(g["m"], g["eps"])
     try:
+        for variant in (1, 2, 3):
+            engine.set_variant(variant)
+            for threads, ipt in ((64, 1), (64, 2), (64, 4), (128, 1), (128, 2), (128, 4), (256, 1), (256, 2)):
+                engine.set_tuning(threads, ipt, 0)
+                st = err_stats(engine.forces(g["x"], S.params(S.R3), S.MIXED), g["F"])
+                assert st["p99"] < MIXED_P99, (variant, threads, ipt, st)
         engine.set_variant(1)
-        for threads, ipt in ((64, 1), (64, 2), (64, 4), (128, 1), (128, 2), (128, 4), (256, 1), (256, 2)):
-            engine.set_tuning(threads, ipt, 0)
-            st = err_stats(engine.forces(g["x"], S.params(S.R3), S.MIXED), g["F"])
-            assert st["p99"] < MIXED_P99, (threads, ipt, st)
         engine.set_tuning(128, 2, 0)
         lo, hi = (int(v) for v in g["sub"])
         assert err_stats(engine.forces(g["x"], S.params(S.R3), S.MIXED, lo, hi), g["F_sub"])["p99"] < MIXED_P99

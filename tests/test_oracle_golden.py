@@ -152,3 +152,15 @@ def test_t3_lattice_forces_vanish(port):
                     table=g["table"], ngrid=ng, order=4)
     F = port.forces(s, x)
     assert np.abs(F).max() < 1e-12 * (n / (0.2 * L) ** 2)
+
+
+def test_r3_n32768_subset(port):
+    """The N = 32,768 compactified workload, regenerated from its seed, against
+    the reference FP64 build on an i range (the fixture of the FP32 floor)."""
+    from steps_gb300 import workloads as W
+
+    g = golden("ref_fp32")
+    ps = W.r3_compactified(int(g["r3_n"]), float(g["r3_rmax"]), seed=int(g["r3_seed"]))
+    lo, hi = (int(v) for v in g["r3_sub"])
+    s = port.system(0, ps.m, ps.eps, port_params(O))
+    assert rel_err(port.forces(s, ps.x, lo, hi), g["r3_F64"]).max() < TOL
