@@ -44,6 +44,7 @@ struct Batch {
     DevBuf part, counter, err;
     int T = 0, ntiles = 0, nitems = 0, threads = 0, ipt = 0, grid = 0;
     long long graph_kernels = 0;
+    int nmax = 0;  // largest realisation
     bool tuned = false;
     cudaGraphExec_t exec = nullptr;
     int graph_steps = -1;
@@ -184,7 +185,8 @@ void batch_forces(Batch &b)
                                                       b.ts.keys[0].as<unsigned long long>(),
                                                       b.ts.vals[0].as<uint32_t>());
     note_launch("k_batch_keys");
-    sort_pairs(b.ts, b.ntot, st);
+    // realisation bits [51, 64) and the leading Morton bits the largest realisation needs
+    sort_pairs(b.ts, b.ntot, st, std::max(0, 51 - std::min(51, morton_sort_bits(b.nmax))));
     tile_build_range(b.x.as<double>(), b.m64.as<double>(), b.eps64.as<double>(), b.ts.perm(), b.ntot, b.T,
                      b.ts.pack.as<float4>(), b.ts.eps.as<float>(), b.ts.meta.as<float4>(), b.ts.idx.as<uint32_t>(),
                      PAD_J, b.ts.resid.as<float4>(), b.ts.soa.as<float>(), b.tdesc.as<int2>(), b.ntiles, st);
@@ -330,6 +332,7 @@ int steps_gpu_batch_set(int count, const int *n, const double *const *x, const d
                 int o = 0;
                 for (int k = 0; k < a.count; k++) { b.off[k] = o; o += a.n[k]; }
                 b.ntot = o;
+                b.nmax = *std::max_element(b.n.begin(), b.n.end());
                 std::vector<uint16_t> rel(b.ntot);
                 for (int k = 0; k < a.count; k++) std::fill(rel.begin() + b.off[k], rel.begin() + b.off[k] + b.n[k], k);
                 b.x.ensure<double>(3 * (size_t)b.ntot);

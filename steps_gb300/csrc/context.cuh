@@ -62,7 +62,9 @@ Tables device_tables(const KParams &kp);
 constexpr uint32_t PAD_J = 0xffffffffu, PAD_I = 0xfffffffeu;
 void build_tiles(TileSet &ts, const double *x, const double *m64, const double *eps64, int lo, int count, int T,
                  bool reuse, cudaStream_t st, unsigned long long *bbox_scratch, uint32_t pad_id);
-void sort_pairs(TileSet &ts, int n, cudaStream_t st);
+// Stable LSD radix sort of (keys, vals) on key bits [lo_bit, 64).
+void sort_pairs(TileSet &ts, int n, cudaStream_t st, int lo_bit = 0);
+int morton_sort_bits(int n);
 void batch_keys(const double *x, int lo, int count, unsigned long long prefix, unsigned long long *keys, uint32_t *vals,
                 unsigned long long *bbox_scratch, cudaStream_t st);
 void tile_build_range(const double *x, const double *m64, const double *eps64, const uint32_t *perm, int count, int T,

@@ -261,12 +261,24 @@ __global__ void __launch_bounds__(TB_THREADS) k_tile_build(const double *__restr
 
 }  // namespace
 
-void sort_pairs(TileSet &ts, int n, cudaStream_t st)
+// Leading Morton bits that order a set of n particles into compact tiles:
+// 2^(bits/3) cells per axis, at least 2^5 times the mean particle spacing,
+// so clustered sets still see about one particle per cell in dense regions.
+// Bits below are left in input order (the sort is stable).
+int morton_sort_bits(int n)
+{
+    int lg = 0;
+    while ((1LL << lg) < (long long)n) lg++;
+    const int bits = 3 * ((lg + 2) / 3 + 5);
+    return bits < 63 ? bits : 63;
+}
+
+void sort_pairs(TileSet &ts, int n, cudaStream_t st, int lo_bit)
 {
     int nblk = div_up(n, SORT_TILE);
     uint32_t *hist = ts.hist.ensure<uint32_t>((size_t)RADIX * (nblk > 0 ? nblk : 1));
     int cur = 0;
-    for (int shift = 0; shift < 64; shift += RADIX_BITS) {
+    for (int shift = lo_bit / RADIX_BITS * RADIX_BITS; shift < 64; shift += RADIX_BITS) {
         k_hist<<<nblk, SORT_THREADS, 0, st>>>(ts.keys[cur].as<unsigned long long>(), n, shift, hist);
         note_launch("k_hist");
         k_scan<<<1, 1024, 0, st>>>(hist, RADIX * nblk);
@@ -303,7 +315,7 @@ void build_tiles(TileSet &ts, const double *x, const double *m64, const double *
         k_keys<<<div_up(count, 256), 256, 0, st>>>(x, lo, count, bbox_scratch, 21, 0ull, ts.keys[0].as<unsigned long long>(),
                                                   ts.vals[0].as<uint32_t>());
         note_launch("k_keys");
-        sort_pairs(ts, count, st);
+        sort_pairs(ts, count, st, 63 - morton_sort_bits(count));
         ts.lo = lo;
         ts.count = count;
         ts.ordered = true;
