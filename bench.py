@@ -58,7 +58,10 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="cfg1", choices=["cfg0", "cfg1", "cfg2", "cfg3", "cfg4"])
     ap.add_argument("--batch-scale", type=float, default=1.0, help="cfg4: scale every N_k (small test runs)")
-    ap.add_argument("--order", type=int, default=2, help="T^3 interpolation order (2 or 4)")
+    ap.add_argument("--order", type=int, default=2,
+                    help="T^3 interpolation order (2 or 4); S1xR2 table order (0, 2 or 4)")
+    ap.add_argument("--s1-table", action="store_true",
+                    help="cfg2 with the (rho, z) correction table instead of the image sum")
     ap.add_argument("--n", type=int, default=0, help="override the particle count (small profiling cases)")
     ap.add_argument("--fp64-sample", type=int, default=16384, help="i particles timed with the FP64 kernel")
     ap.add_argument("--cpu-sample", type=int, default=0,
@@ -88,13 +91,24 @@ def workload(args, rank=0):
     if w == "cfg2":
         n = args.n or (1 << 21)
         ps = W.s1r2_cylindrical(n, 200.0, 600.0, seed=2 + rank)
+        if args.s1_table:
+            # The (rho, z) table with the reference's IS_PERIODIC = 2 settings
+            # (StePS/src/main.cc:569-602): N_z = 128, N_rho = floor(N_z 2.25 Rsim / L),
+            # alpha L = 0.787875, n_max = 4, m_max = 10; interpolation order --order.
+            nz = 128
+            nrho = int(math.floor(nz * 2.25 * 600.0 / 200.0))
+            p = S.params(S.S1R2, is_periodic=2, L=200.0, rsim=600.0, s1r2_images=0, ewald_order=args.order)
+            table = {"kind": "s1", "args": (nrho, nz, 2.25 * 600.0, 200.0, 0.787875 / 200.0, 4, 10)}
+            flops = 33 + {0: 2, 2: 24, 4: 56}[args.order]  # pair part as T^3 + NGP / CIC / TSC taps
+            return ps, p, flops, (f"S1xR2 N={n} L_z=200 Mpc R_max=600 Mpc, (rho, z) correction table "
+                                           f"{nrho}x{nz} order {args.order} (IS_PERIODIC=2)"), table
         p = S.params(S.S1R2, is_periodic=2, L=200.0, rsim=600.0, s1r2_images=1)
         return ps, p, 11 + 11 * 7, f"S1xR2 N={n} L_z=200 Mpc R_max=600 Mpc, 7 z images (IS_PERIODIC=2)", None
     n = args.n or (1 << 19)
     ps = W.t3_clumpy(n, 100.0, seed=3 + rank)
     p = S.params(S.T3, is_periodic=2, L=100.0, rsim=50.0, ewald_order=args.order)
     flops = 33 + (494 if args.order == 4 else 62)
-    table = (T3_NG, 100.0, 2.0 / 100.0, 2.0, 5.0 * 2.0 * math.pi / 100.0, 3.0, 6.0)
+    table = {"kind": "t3", "args": (T3_NG, 100.0, 2.0 / 100.0, 2.0, 5.0 * 2.0 * math.pi / 100.0, 3.0, 6.0)}
     return ps, p, flops, f"T3 N={n} L=100 Mpc clumpy, Ewald table Ng={T3_NG} order {args.order}", table
 
 
@@ -175,7 +189,7 @@ class ClockSampler:
                 "samples": len(self.rows)}
 
 
-def cpu_baseline(ps, p, sample: int, threads: int, table=None, ngrid=0, seconds: float = 10.0):
+def cpu_baseline(ps, p, sample: int, threads: int, table=None, seconds: float = 10.0):
     """The reference algorithm on the host cores: the plain-C oracle (OpenMP
     over i, sequential j, per-pair atomics, as StePS/src/forces.cc), timed on
     the i range [N/2, N/2 + sample) against all N j. sample <= 0 sizes the
@@ -184,9 +198,10 @@ def cpu_baseline(ps, p, sample: int, threads: int, table=None, ngrid=0, seconds:
     import pyoracle
 
     port = pyoracle.Port(threads=threads)
-    tp = {0: 0, 1: 1, 2: 3}[p.topology]
-    s = port.system(tp, ps.m, ps.eps, pyoracle.make_params(p.is_periodic, p.L, p.rsim), table=table, ngrid=ngrid,
-                    order=p.ewald_order)
+    tp = {0: 0, 1: 1, 2: 3 if p.s1r2_images else 2}[p.topology]
+    tab, ng, nrho, nz = table if table else (None, 0, 0, 0)
+    s = port.system(tp, ps.m, ps.eps, pyoracle.make_params(p.is_periodic, p.L, p.rsim), table=tab, ngrid=ng,
+                    nrho=nrho, nz=nz, order=p.ewald_order)
     lo = ps.n // 2
     probe = min(max(threads, 8), ps.n - lo)
     port.forces(s, ps.x, lo, lo + probe - 1)  # warm-up: threads, pages
@@ -209,24 +224,38 @@ def cpu_baseline(ps, p, sample: int, threads: int, table=None, ngrid=0, seconds:
     return pairs / dt, dt, pairs, hi - lo + 1
 
 
-def host_table(table):
-    """The T^3 table for the CPU baseline (the oracle's builder, on the host)."""
+def host_table(table, eng=None):
+    """The workload's Ewald table for the CPU baseline as (table, ngrid, nrho, nz):
+    the GPU-built table when an engine holds it (the builders match the
+    reference's to 1e-13), else the oracle's builder on the host."""
+    if table is None:
+        return None
+    if table["kind"] == "t3":
+        ng = table["args"][0]
+        if eng is not None:
+            return eng.get_table_t3(ng), ng, 0, 0
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import pyoracle
+
+        return pyoracle.Port().t3_table(*table["args"]), ng, 0, 0
+    nrho, nz = table["args"][:2]
+    if eng is not None:
+        return eng.get_table_s1r2(nrho, nz), 0, nrho, nz
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
 
-    ng, L, alpha, rel, rec, rr, kr = table
-    return pyoracle.Port().t3_table(ng, L, alpha, rel, rec, rr, kr), ng
+    return pyoracle.Port().s1r2_table(*table["args"]), 0, nrho, nz
 
 
 def run_reference(args, ws, rank):
     if rank != 0:
         return
     ps, p, flops, desc, table = workload(args)
-    tab, ng = host_table(table) if table else (None, 0)
+    tab = host_table(table)
     threads = os.cpu_count() or 1
     for _ in range(max(args.warmup, 0)):
-        cpu_baseline(ps, p, 0, threads, tab, ng, seconds=args.cpu_seconds / 8)
-    runs = [cpu_baseline(ps, p, args.cpu_sample, threads, tab, ng, seconds=args.cpu_seconds)
+        cpu_baseline(ps, p, 0, threads, tab, seconds=args.cpu_seconds / 8)
+    runs = [cpu_baseline(ps, p, args.cpu_sample, threads, tab, seconds=args.cpu_seconds)
             for _ in range(args.steps)]
     v = float(np.median([r[0] for r in runs]))
     sample = runs[0][3]
@@ -248,8 +277,10 @@ def run_ours(args, ws, rank, local, dist):
     n = ps.n
     eng = S.Engine(local)
     eng.set_particles(ps.m, ps.eps)
-    if table:
-        eng.build_table_t3(*table)
+    if table and table["kind"] == "t3":
+        eng.build_table_t3(*table["args"])
+    elif table:
+        eng.build_table_s1r2(*table["args"])
     eng.upload_positions(ps.x)
     f32_peak, f64_peak = eng.measure_peaks()
     if args.variant >= 0:
@@ -343,7 +374,7 @@ def run_ours(args, ws, rank, local, dist):
         "gpu_launches": int(launches),
         "clocks": clk,
     }
-    return line, ps, p, table
+    return line, ps, p, host_table(table, eng)
 
 
 def run_batch(args, ws, rank, local, dist):
@@ -425,11 +456,10 @@ def main():
         if dist is not None:
             dist.destroy_process_group()
         return
-    line, ps, p, table = run_ours(args, ws, rank, local, dist)
+    line, ps, p, tab = run_ours(args, ws, rank, local, dist)
     if rank == 0:
         threads = os.cpu_count() or 1
-        tab, ng = host_table(table) if table else (None, 0)
-        rate, dt, pairs, ni = cpu_baseline(ps, p, args.cpu_sample, threads, tab, ng, seconds=args.cpu_seconds)
+        rate, dt, pairs, ni = cpu_baseline(ps, p, args.cpu_sample, threads, tab, seconds=args.cpu_seconds)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                                 "sample": f"{ni} i particles x all {ps.n} j ({dt:.1f} s of CPU work)"}
         print(json.dumps(line), flush=True)

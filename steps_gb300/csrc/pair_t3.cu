@@ -329,6 +329,17 @@ __global__ void __launch_bounds__(BLOCK) k_pair_t3(MixedArgs a)
     }
 }
 
+// Cell index of a nearest-image z in [-L/2, L/2]: floor(uz) lies in [-1, nz]
+// up to rounding, so one conditional shift wraps it; anything else
+// (non-finite input) is clamped into [0, nz).
+__device__ __forceinline__ int wrap_near(float f, int nz)
+{
+    int i = (int)f;
+    i += i < 0 ? nz : 0;
+    i -= i >= nz ? nz : 0;
+    return min(max(i, 0), nz - 1);
+}
+
 // (rho, z) table interpolation in FP32 from the float2 copy of the S1xR2
 // table: NGP / CIC / TSC exactly as StePS/src/ewald_space.cc:803-1000
 // (rho clamped to [0, rho_max], z index periodic).
@@ -345,7 +356,7 @@ __device__ __forceinline__ void s1r2_interp_f32(const float2 *__restrict__ T, in
     if (ORDER == 0) {
         int ir = (int)floorf(ur + 0.5f);
         ir = ir < 0 ? 0 : (ir > nrho - 1 ? nrho - 1 : ir);
-        const int izc = pmod((int)floorf(uz + 0.5f), nz);
+        const int izc = wrap_near(floorf(uz + 0.5f), nz);
         const float2 v = __ldg(T + (size_t)ir * nz + izc);
         Dr = v.x;
         Dz = v.y;
@@ -354,9 +365,9 @@ __device__ __forceinline__ void s1r2_interp_f32(const float2 *__restrict__ T, in
         float fr = ur - (float)ir0;
         if (ir0 < 0) { ir0 = 0; fr = 0.0f; }
         if (ir0 > nrho - 2) { ir0 = nrho - 2 > 0 ? nrho - 2 : 0; fr = 1.0f; }
-        const int iz0f = (int)floorf(uz);
-        const float fz = uz - (float)iz0f;
-        const int iz0 = pmod(iz0f, nz), iz1 = pmod(iz0 + 1, nz);
+        const float iz0r = floorf(uz);
+        const float fz = uz - iz0r;
+        const int iz0 = wrap_near(iz0r, nz), iz1 = iz0 + 1 < nz ? iz0 + 1 : 0;
         const float2 a00 = __ldg(T + (size_t)ir0 * nz + iz0), a10 = __ldg(T + (size_t)(ir0 + 1) * nz + iz0);
         const float2 a01 = __ldg(T + (size_t)ir0 * nz + iz1), a11 = __ldg(T + (size_t)(ir0 + 1) * nz + iz1);
         const float w00 = (1.0f - fr) * (1.0f - fz), w10 = fr * (1.0f - fz), w01 = (1.0f - fr) * fz, w11 = fr * fz;
@@ -372,9 +383,11 @@ __device__ __forceinline__ void s1r2_interp_f32(const float2 *__restrict__ T, in
         if (ir[1] < 0) ir[1] = 0;
         if (ir[1] > nrho - 1) ir[1] = nrho - 1;
         if (ir[2] > nrho - 1) ir[2] = nrho - 1;
+        const int iz1 = wrap_near((float)jz, nz);
+        const int izs[3] = {iz1 > 0 ? iz1 - 1 : nz - 1, iz1, iz1 + 1 < nz ? iz1 + 1 : 0};
 #pragma unroll
         for (int c = 0; c < 3; c++) {
-            const int izc = pmod(jz - 1 + c, nz);
+            const int izc = izs[c];
 #pragma unroll
             for (int r = 0; r < 3; r++) {
                 const float2 v = __ldg(T + (size_t)ir[r] * nz + izc);

@@ -80,6 +80,26 @@ def test_s1r2_table_fp64(engine, order):
     assert rel_err(F, g["F"]).max() < FP64_TOL
 
 
+@pytest.mark.parametrize("order", [0, 2, 4])
+def test_s1r2_table_mixed(engine, order):
+    """The (rho, z) table mode in mixed precision against the reference, every
+    kernel shape, full range and an i subset."""
+    g = golden(f"s1r2_table_o{order}")
+    nrho, nz = (int(v) for v in g["shape"])
+    engine.set_particles(g["m"], g["eps"])
+    engine.set_table_s1r2(g["table"], nrho, nz)
+    p = s1_params(g, 2, images=0, order=order)
+    try:
+        for threads, ipt in ((64, 1), (64, 2), (128, 1), (128, 2), (256, 1)):
+            engine.set_tuning(threads, ipt, 0)
+            st = err_stats(engine.forces(g["x"], p, S.MIXED), g["F"])
+            assert st["p99"] < MIXED_P99, (order, threads, ipt, st)
+    finally:
+        engine.set_tuning(128, 2, 0)
+    st = err_stats(engine.forces(g["x"], p, S.MIXED, 500, 1200), g["F"][500:1201])
+    assert st["p99"] < MIXED_P99, st
+
+
 def test_s1r2_table_builder(engine):
     g = golden("s1r2_table_o2")
     nrho, nz = (int(v) for v in g["shape"])
