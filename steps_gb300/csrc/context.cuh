@@ -34,6 +34,8 @@ struct Ctx {
     long long t3_version = 0;  // bumped whenever the table changes
     DevBuf t3f;                // FP32 float4-per-cell haloed copy for the mixed kernels
     long long t3f_version = -1;
+    DevBuf t3r;                // tricubic z-row records of the haloed copy
+    long long t3r_version = -1;
     DevBuf s1r2;
     int nrho = 0, nz = 0;
     long long s1r2_version = 0;

@@ -42,6 +42,7 @@ struct MixedArgs {
     float ih, u0;       // continuous cell index u(d) = d * ih + u0, ih = ng / L, u0 = ng/2 - 1/2
     int wcap;           // cells of the shared-memory table window
     int halo, ext;      // the FP32 copy is haloed: ext^3 cells, ext = ng + 2 halo
+    const float4 *t3r;  // tricubic: z-row records of the haloed copy (3 float4 per cell)
     // S1xR2 (rho, z) correction table (FP32 float2 copy) and its geometry
     const float2 *s1tab;
     int nrho, nz;

@@ -480,6 +480,7 @@ void forces_mixed(const KParams &kp, const Tables &tb, const double *x, const do
     a.ih = a.u0 = 0.0f;
     a.wcap = 0;
     a.halo = a.ext = 0;
+    a.t3r = nullptr;
     a.s1tab = nullptr;
     a.nrho = a.nz = 0;
     a.irho = a.iz = a.rho_max = 0.0f;

@@ -56,13 +56,45 @@ __device__ __forceinline__ void weights(float t, float *w)
     }
 }
 
+// w . v for the 4 z taps of a z-row record.
+__device__ __forceinline__ float dot4(const float *w, float4 v)
+{
+    return fmaf(w[3], v.w, fmaf(w[2], v.z, fmaf(w[1], v.y, w[0] * v.x)));
+}
+
 // Sum of the NT^3 stencil taps fetch(a, b, c) weighted by wx[a] wy[b] wz[c].
+// Trilinear: 8 products of the three weights (36 FP ops). Tricubic: nested,
+// sum_a wx_a sum_b wy_b sum_c wz_c T_abc (252 FP ops instead of 272).
 template <int ORDER, class Fetch>
 __device__ __forceinline__ void stencil(const float *wx, const float *wy, const float *wz, Fetch fetch, float &Dx,
                                         float &Dy, float &Dz)
 {
     constexpr int NT = ORDER;
-#pragma unroll(ORDER == 4 ? 1 : NT)
+    if (ORDER == 4) {
+#pragma unroll
+        for (int aa = 0; aa < NT; aa++) {
+            float rx = 0.0f, ry = 0.0f, rz = 0.0f;
+#pragma unroll
+            for (int bb = 0; bb < NT; bb++) {
+                float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+#pragma unroll
+                for (int cc = 0; cc < NT; cc++) {
+                    const float4 v = fetch(aa, bb, cc);
+                    sx = fmaf(wz[cc], v.x, sx);
+                    sy = fmaf(wz[cc], v.y, sy);
+                    sz = fmaf(wz[cc], v.z, sz);
+                }
+                rx = fmaf(wy[bb], sx, rx);
+                ry = fmaf(wy[bb], sy, ry);
+                rz = fmaf(wy[bb], sz, rz);
+            }
+            Dx = fmaf(wx[aa], rx, Dx);
+            Dy = fmaf(wx[aa], ry, Dy);
+            Dz = fmaf(wx[aa], rz, Dz);
+        }
+        return;
+    }
+#pragma unroll
     for (int aa = 0; aa < NT; aa++)
 #pragma unroll
         for (int bb = 0; bb < NT; bb++) {
@@ -274,10 +306,31 @@ __global__ void __launch_bounds__(BLOCK) k_pair_t3(MixedArgs a)
                             bx = min(max((int)fxl - OFF, 0), E - NT);
                             by = min(max((int)fyl - OFF, 0), E - NT);
                             bz = min(max((int)fzl - OFF, 0), E - NT);
-                            const float4 *base = a.t3f + ((bx * E + by) * E + bz);
-                            stencil<ORDER>(wx, wy, wz,
-                                           [&](int aa, int bb, int cc) { return __ldg(base + (aa * E + bb) * E + cc); },
-                                           Dx, Dy, Dz);
+                            if (ORDER == 4) {
+                                // z-row records: the 4 z taps of one (x, y) row, per
+                                // component, in 3 float4 (48 B), 16 rows per pair
+                                const float4 *rbase = a.t3r + 3 * ((bx * E + by) * E + bz);
+#pragma unroll
+                                for (int aa = 0; aa < 4; aa++) {
+                                    float rx = 0.0f, ry = 0.0f, rz = 0.0f;
+#pragma unroll
+                                    for (int bb = 0; bb < 4; bb++) {
+                                        const float4 *r = rbase + 3 * (aa * E + bb) * E;
+                                        const float4 vx = __ldg(r), vy = __ldg(r + 1), vz = __ldg(r + 2);
+                                        rx = fmaf(wy[bb], dot4(wz, vx), rx);
+                                        ry = fmaf(wy[bb], dot4(wz, vy), ry);
+                                        rz = fmaf(wy[bb], dot4(wz, vz), rz);
+                                    }
+                                    Dx = fmaf(wx[aa], rx, Dx);
+                                    Dy = fmaf(wx[aa], ry, Dy);
+                                    Dz = fmaf(wx[aa], rz, Dz);
+                                }
+                            } else {
+                                const float4 *base = a.t3f + ((bx * E + by) * E + bz);
+                                stencil<ORDER>(
+                                    wx, wy, wz, [&](int aa, int bb, int cc) { return __ldg(base + (aa * E + bb) * E + cc); },
+                                    Dx, Dy, Dz);
+                            }
                         } else {  // wrapped lookup (tile pairs wider than the halo)
                             const float ux = fmaf(dx, a.ih, a.u0), uy = fmaf(dy, a.ih, a.u0),
                                         uz = fmaf(dz, a.ih, a.u0);
@@ -583,6 +636,24 @@ KernelFn t3_kernel(const KParams &kp, int threads, int ipt, size_t *dyn_smem)
     return kp.order == 4 ? pick_t3<4>(threads, ipt) : pick_t3<2>(threads, ipt);
 }
 
+// z-row records of the haloed table: record (i, j, k) of the ext^3 grid holds
+// cells (i, j, k..k+3) as 3 float4, one per component (x taps, y taps, z taps).
+__global__ void k_table_zrow(const double *__restrict__ t, int ng, int halo, float4 *__restrict__ out)
+{
+    const int ext = ng + 2 * halo;
+    const size_t ncell = (size_t)ext * ext * ext;
+    size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncell) return;
+    const int k = (int)(c % ext), j = (int)((c / ext) % ext), i = (int)(c / ((size_t)ext * ext));
+    const size_t row = ((size_t)pmod(i - halo, ng) * ng + pmod(j - halo, ng)) * ng;
+    float v[3][4];
+    for (int q = 0; q < 4; q++) {
+        const size_t s = row + pmod(k + q - halo, ng);
+        for (int comp = 0; comp < 3; comp++) v[comp][q] = (float)t[3 * s + comp];
+    }
+    for (int comp = 0; comp < 3; comp++) out[3 * c + comp] = make_float4(v[comp][0], v[comp][1], v[comp][2], v[comp][3]);
+}
+
 // Halo of the FP32 table copy: tile pairs whose stencils stay within it need
 // no per-pair index wrap.
 constexpr int T3_HALO = 16;
@@ -602,6 +673,21 @@ const float4 *t3_table_f32(const Tables &tb, cudaStream_t st)
     return c.t3f.as<float4>();
 }
 
+// The z-row records for tricubic tables, rebuilt whenever the table changes.
+const float4 *t3_table_zrow(const Tables &tb, cudaStream_t st)
+{
+    Ctx &c = ctx();
+    const size_t ext = (size_t)tb.t3_ng + 2 * T3_HALO;
+    const size_t ncell = ext * ext * ext;
+    if (c.t3r_version != c.t3_version || !c.t3r.p) {
+        float4 *o = c.t3r.ensure<float4>(3 * ncell);
+        k_table_zrow<<<(unsigned)((ncell + 255) / 256), 256, 0, st>>>(tb.t3, tb.t3_ng, T3_HALO, o);
+        note_launch("k_table_zrow");
+        c.t3r_version = c.t3_version;
+    }
+    return c.t3r.as<float4>();
+}
+
 void t3_args(MixedArgs &a, const KParams &kp, const Tables &tb, cudaStream_t st)
 {
     a.t3f = nullptr;
@@ -611,8 +697,10 @@ void t3_args(MixedArgs &a, const KParams &kp, const Tables &tb, cudaStream_t st)
     a.wcap = ctx().shape.t3_cells;
     a.halo = T3_HALO;
     a.ext = tb.t3_ng + 2 * T3_HALO;
+    a.t3r = nullptr;
     if (kp.is_periodic >= 2) {
         a.t3f = t3_table_f32(tb, st);
+        if (kp.order == 4) a.t3r = t3_table_zrow(tb, st);
         a.ih = (float)((double)tb.t3_ng / kp.L);
         a.u0 = (float)((double)tb.t3_ng * 0.5 - 0.5);
     }
