@@ -36,6 +36,8 @@ struct Ctx {
     long long t3f_version = -1;
     DevBuf t3r;                // tricubic z-row records of the haloed copy
     long long t3r_version = -1;
+    DevBuf s1rec;              // S1xR2 table z-triplet records (CIC, TSC)
+    long long s1rec_version = -1;
     DevBuf s1r2;
     int nrho = 0, nz = 0;
     long long s1r2_version = 0;

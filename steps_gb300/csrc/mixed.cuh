@@ -45,6 +45,7 @@ struct MixedArgs {
     const float4 *t3r;  // tricubic: z-row records of the haloed copy (3 float4 per cell)
     // S1xR2 (rho, z) correction table (FP32 float2 copy) and its geometry
     const float2 *s1tab;
+    const float4 *s1rec;  // z-triplet records of s1tab (CIC, TSC)
     int nrho, nz;
     float irho, iz, rho_max;  // 1 / drho, nz / L_z
 };

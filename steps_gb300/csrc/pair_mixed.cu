@@ -482,6 +482,7 @@ void forces_mixed(const KParams &kp, const Tables &tb, const double *x, const do
     a.halo = a.ext = 0;
     a.t3r = nullptr;
     a.s1tab = nullptr;
+    a.s1rec = nullptr;
     a.nrho = a.nz = 0;
     a.irho = a.iz = a.rho_max = 0.0f;
     if (kp.topology == STEPS_T3) t3_args(a, kp, tb, st);

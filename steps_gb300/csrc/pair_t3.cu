@@ -396,10 +396,14 @@ __device__ __forceinline__ int wrap_near(float f, int nz)
 // (rho, z) table interpolation in FP32 from the float2 copy of the S1xR2
 // table: NGP / CIC / TSC exactly as StePS/src/ewald_space.cc:803-1000
 // (rho clamped to [0, rho_max], z index periodic).
+// CIC and TSC read z-triplet records R: record (ir, iz) = cells (ir, iz-1),
+// (ir, iz), (ir, iz+1), z periodic, as (Dr, Dz) pairs in 2 float4 (the last
+// two floats unused). One rho row of a stencil is then 1 (CIC) or 2 (TSC)
+// loads instead of 2 or 3.
 template <int ORDER>
-__device__ __forceinline__ void s1r2_interp_f32(const float2 *__restrict__ T, int nrho, int nz, float irho,
-                                                float rho_max, float iz, float halfL, float rho, float z, float &Dr,
-                                                float &Dz)
+__device__ __forceinline__ void s1r2_interp_f32(const float2 *__restrict__ T, const float4 *__restrict__ R, int nrho,
+                                                int nz, float irho, float rho_max, float iz, float halfL, float rho,
+                                                float z, float &Dr, float &Dz)
 {
     const float rr = fminf(fmaxf(rho, 0.0f), rho_max);
     const float ur = rr * irho;
@@ -421,11 +425,11 @@ __device__ __forceinline__ void s1r2_interp_f32(const float2 *__restrict__ T, in
         const float iz0r = floorf(uz);
         const float fz = uz - iz0r;
         const int iz0 = wrap_near(iz0r, nz), iz1 = iz0 + 1 < nz ? iz0 + 1 : 0;
-        const float2 a00 = __ldg(T + (size_t)ir0 * nz + iz0), a10 = __ldg(T + (size_t)(ir0 + 1) * nz + iz0);
-        const float2 a01 = __ldg(T + (size_t)ir0 * nz + iz1), a11 = __ldg(T + (size_t)(ir0 + 1) * nz + iz1);
+        // record (ir, iz0 + 1) starts with cells iz0, iz0 + 1
+        const float4 r0 = __ldg(R + 2 * ((size_t)ir0 * nz + iz1)), r1 = __ldg(R + 2 * ((size_t)(ir0 + 1) * nz + iz1));
         const float w00 = (1.0f - fr) * (1.0f - fz), w10 = fr * (1.0f - fz), w01 = (1.0f - fr) * fz, w11 = fr * fz;
-        Dr = w00 * a00.x + w10 * a10.x + w01 * a01.x + w11 * a11.x;
-        Dz = w00 * a00.y + w10 * a10.y + w01 * a01.y + w11 * a11.y;
+        Dr = w00 * r0.x + w10 * r1.x + w01 * r0.z + w11 * r1.z;
+        Dz = w00 * r0.y + w10 * r1.y + w01 * r0.w + w11 * r1.w;
     } else {
         const int jr = (int)floorf(ur + 0.5f), jz = (int)floorf(uz + 0.5f);
         const float sr = ur - (float)jr, sz = uz - (float)jz;
@@ -437,17 +441,14 @@ __device__ __forceinline__ void s1r2_interp_f32(const float2 *__restrict__ T, in
         if (ir[1] > nrho - 1) ir[1] = nrho - 1;
         if (ir[2] > nrho - 1) ir[2] = nrho - 1;
         const int iz1 = wrap_near((float)jz, nz);
-        const int izs[3] = {iz1 > 0 ? iz1 - 1 : nz - 1, iz1, iz1 + 1 < nz ? iz1 + 1 : 0};
 #pragma unroll
-        for (int c = 0; c < 3; c++) {
-            const int izc = izs[c];
-#pragma unroll
-            for (int r = 0; r < 3; r++) {
-                const float2 v = __ldg(T + (size_t)ir[r] * nz + izc);
-                const float w = wr[r] * wz[c];
-                Dr = fmaf(w, v.x, Dr);
-                Dz = fmaf(w, v.y, Dz);
-            }
+        for (int r = 0; r < 3; r++) {  // record (ir, iz1): cells iz1 - 1, iz1, iz1 + 1
+            const float4 *rec = R + 2 * ((size_t)ir[r] * nz + iz1);
+            const float4 v01 = __ldg(rec), v2 = __ldg(rec + 1);
+            const float sr_ = fmaf(wz[2], v2.x, fmaf(wz[1], v01.z, wz[0] * v01.x));
+            const float sz_ = fmaf(wz[2], v2.y, fmaf(wz[1], v01.w, wz[0] * v01.y));
+            Dr = fmaf(wr[r], sr_, Dr);
+            Dz = fmaf(wr[r], sz_, Dz);
         }
     }
 }
@@ -559,7 +560,7 @@ __global__ void __launch_bounds__(BLOCK) k_pair_s1tab(MixedArgs a)
                     }
                     const float rho = sqrt_mufu(rho2);
                     float Dr, Dz;
-                    s1r2_interp_f32<ORDER>(tab, a.nrho, a.nz, irho, rho_max, iz, halfL, rho, dz, Dr, Dz);
+                    s1r2_interp_f32<ORDER>(tab, a.s1rec, a.nrho, a.nz, irho, rho_max, iz, halfL, rho, dz, Dr, Dz);
                     const float er = rho > 0.0f ? Dr * rcp_mufu(rho) : 0.0f;
                     fx[k] = fmaf(q.w, fmaf(w, dx, -er * dx), fx[k]);
                     fy[k] = fmaf(q.w, fmaf(w, dy, -er * dy), fy[k]);
@@ -584,6 +585,19 @@ __global__ void __launch_bounds__(BLOCK) k_pair_s1tab(MixedArgs a)
             o[3 * q + 2] = az[k];
         }
     }
+}
+
+// z-triplet records of the (rho, z) table (see s1r2_interp_f32).
+__global__ void k_table2_zrec(const double *__restrict__ t, int nrho, int nz, float4 *__restrict__ out)
+{
+    const size_t ncell = (size_t)nrho * nz;
+    size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncell) return;
+    const int iz = (int)(c % nz);
+    const size_t row = c - iz;
+    const size_t m = row + (iz > 0 ? iz - 1 : nz - 1), p = row + (iz + 1 < nz ? iz + 1 : 0);
+    out[2 * c] = make_float4((float)t[2 * m], (float)t[2 * m + 1], (float)t[2 * c], (float)t[2 * c + 1]);
+    out[2 * c + 1] = make_float4((float)t[2 * p], (float)t[2 * p + 1], 0.0f, 0.0f);
 }
 
 __global__ void k_table2_f32(const double *__restrict__ t, size_t ncell, float2 *__restrict__ out)
@@ -723,7 +737,14 @@ void s1tab_args(MixedArgs &a, const KParams &kp, const Tables &tb, cudaStream_t 
         note_launch("k_table2_f32");
         c.s1f_version = c.s1r2_version;
     }
+    if (kp.order != 0 && (c.s1rec_version != c.s1r2_version || !c.s1rec.p)) {
+        float4 *o = c.s1rec.ensure<float4>(2 * ncell);
+        k_table2_zrec<<<(unsigned)((ncell + 255) / 256), 256, 0, st>>>(tb.s1r2, tb.nrho, tb.nz, o);
+        note_launch("k_table2_zrec");
+        c.s1rec_version = c.s1r2_version;
+    }
     a.s1tab = c.s1f.as<float2>();
+    a.s1rec = kp.order != 0 ? c.s1rec.as<float4>() : nullptr;
     a.nrho = tb.nrho;
     a.nz = tb.nz;
     const double drho = tb.rho_max / (double)(tb.nrho - 1 > 1 ? tb.nrho - 1 : 1);
