@@ -34,8 +34,9 @@ struct Ctx {
     long long t3_version = 0;  // bumped whenever the table changes
     DevBuf t3f;                // FP32 float4-per-cell haloed copy for the mixed kernels
     long long t3f_version = -1;
-    DevBuf t3r;                // tricubic z-row records of the haloed copy
+    DevBuf t3r;                // stencil records of the haloed copy (z rows / yz quads)
     long long t3r_version = -1;
+    int t3r_order = 0;
     DevBuf s1rec;              // S1xR2 table z-triplet records (CIC, TSC)
     long long s1rec_version = -1;
     DevBuf s1r2;

@@ -42,12 +42,13 @@ struct MixedArgs {
     float ih, u0;       // continuous cell index u(d) = d * ih + u0, ih = ng / L, u0 = ng/2 - 1/2
     int wcap;           // cells of the shared-memory table window
     int halo, ext;      // the FP32 copy is haloed: ext^3 cells, ext = ng + 2 halo
-    const float4 *t3r;  // tricubic: z-row records of the haloed copy (3 float4 per cell)
+    const float4 *t3r;  // stencil records of the haloed copy (3 float4 per cell)
     // S1xR2 (rho, z) correction table (FP32 float2 copy) and its geometry
     const float2 *s1tab;
     const float4 *s1rec;  // z-triplet records of s1tab (CIC, TSC)
     int nrho, nz;
     float irho, iz, rho_max;  // 1 / drho, nz / L_z
+    double s1_rho_max, s1_idrho, s1_idz, s1_L;  // the same in FP64 (exact NGP decisions)
 };
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem)

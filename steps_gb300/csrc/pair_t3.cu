@@ -326,10 +326,19 @@ __global__ void __launch_bounds__(BLOCK) k_pair_t3(MixedArgs a)
                                     Dz = fmaf(wx[aa], rz, Dz);
                                 }
                             } else {
-                                const float4 *base = a.t3f + ((bx * E + by) * E + bz);
-                                stencil<ORDER>(
-                                    wx, wy, wz, [&](int aa, int bb, int cc) { return __ldg(base + (aa * E + bb) * E + cc); },
-                                    Dx, Dy, Dz);
+                                // (y, z) quad records: cells (x, y..y+1, z..z+1), per
+                                // component, in 3 float4 (48 B), 2 records per pair
+                                const float q00 = wy[0] * wz[0], q01 = wy[0] * wz[1], q10 = wy[1] * wz[0],
+                                            q11 = wy[1] * wz[1];
+                                const float4 *rbase = a.t3r + 3 * ((bx * E + by) * E + bz);
+#pragma unroll
+                                for (int aa = 0; aa < 2; aa++) {
+                                    const float4 *r = rbase + 3 * aa * E * E;
+                                    const float4 vx = __ldg(r), vy = __ldg(r + 1), vz = __ldg(r + 2);
+                                    Dx = fmaf(wx[aa], fmaf(q11, vx.w, fmaf(q10, vx.z, fmaf(q01, vx.y, q00 * vx.x))), Dx);
+                                    Dy = fmaf(wx[aa], fmaf(q11, vy.w, fmaf(q10, vy.z, fmaf(q01, vy.y, q00 * vy.x))), Dy);
+                                    Dz = fmaf(wx[aa], fmaf(q11, vz.w, fmaf(q10, vz.z, fmaf(q01, vz.y, q00 * vz.x))), Dz);
+                                }
                             }
                         } else {  // wrapped lookup (tile pairs wider than the halo)
                             const float ux = fmaf(dx, a.ih, a.u0), uy = fmaf(dy, a.ih, a.u0),
@@ -453,6 +462,29 @@ __device__ __forceinline__ void s1r2_interp_f32(const float2 *__restrict__ T, co
     }
 }
 
+// The separation (q + ql) - (ph + pl) of a double-float pair in FP64 (exact
+// up to the FP64 rounding of the sum).
+__device__ __forceinline__ double exact_sep(float q, float ph, float ql, float pl)
+{
+    float e;
+    const float s = two_diff(q, ph, e);
+    return (double)s + ((double)e + ((double)ql - (double)pl));
+}
+
+// NGP cell of the separation (dx, dy, dz), dz already the nearest image, in
+// FP64 as StePS/src/ewald_space.cc:803-840 computes it (up to 1 ulp in the
+// scaled indices).
+__device__ __forceinline__ void ngp_index_fp64(double dx, double dy, double dz, const MixedArgs &a, int &ir, int &iz)
+{
+    double rho = sqrt(dx * dx + dy * dy);
+    rho = rho < 0.0 ? 0.0 : (rho > a.s1_rho_max ? a.s1_rho_max : rho);
+    // products with the FP64 reciprocals: within 1 ulp of the reference's quotients
+    const double ur = rho * a.s1_idrho;
+    const double uz = (dz + 0.5 * a.s1_L) * a.s1_idz - 0.5;
+    ir = min(max((int)floor(ur + 0.5), 0), a.nrho - 1);
+    iz = wrap_near((float)floor(uz + 0.5), a.nz);
+}
+
 // S1xR2 with the (rho, z) correction table (StePS/src/forces.cc:1307-1350):
 // nearest image along z, softened Newton, minus m_j D(rho, dz).
 template <int BLOCK, int IPT, int ORDER>
@@ -560,7 +592,32 @@ __global__ void __launch_bounds__(BLOCK) k_pair_s1tab(MixedArgs a)
                     }
                     const float rho = sqrt_mufu(rho2);
                     float Dr, Dz;
-                    s1r2_interp_f32<ORDER>(tab, a.s1rec, a.nrho, a.nz, irho, rho_max, iz, halfL, rho, dz, Dr, Dz);
+                    if (ORDER == 0) {
+                        // NGP picks a cell, a hard decision: within FP32 rounding of
+                        // a cell face it is taken on the FP64 separation, with the
+                        // reference's own arithmetic (StePS/src/ewald_space.cc:803-840).
+                        const float ur = fminf(fmaxf(rho, 0.0f), rho_max) * irho + 0.5f;
+                        const float uzc = (dz + halfL) * iz;
+                        const float fr = ur - floorf(ur), fz = uzc - floorf(uzc);
+                        // FP32 (rho, z) carry < 3e-7 relative error; margin 2x
+                        const float tr = 6e-7f * ur + 2e-6f, tz = 6e-7f * uzc + 2e-6f;
+                        int ir, izc;
+                        if (!self && (fr < tr || fr > 1.0f - tr || fz < tz || fz > 1.0f - tz)) {
+                            const double dx64 = exact_sep(q.x, phx[k], ql.x, plx[k]);
+                            const double dy64 = exact_sep(q.y, phy[k], ql.y, ply[k]);
+                            double dz64 = exact_sep(q.z, phz[k], ql.z, plz[k]);
+                            if (dz != (q.z - phz[k]) + (ql.z - plz[k])) dz64 -= copysign(a.s1_L, dz64);  // wrapped
+                            ngp_index_fp64(dx64, dy64, dz64, a, ir, izc);
+                        } else {
+                            ir = min(max((int)floorf(ur), 0), a.nrho - 1);
+                            izc = wrap_near(floorf(uzc), a.nz);
+                        }
+                        const float2 v = __ldg(tab + (size_t)ir * a.nz + izc);
+                        Dr = v.x;
+                        Dz = v.y;
+                    } else {
+                        s1r2_interp_f32<ORDER>(tab, a.s1rec, a.nrho, a.nz, irho, rho_max, iz, halfL, rho, dz, Dr, Dz);
+                    }
                     const float er = rho > 0.0f ? Dr * rcp_mufu(rho) : 0.0f;
                     fx[k] = fmaf(q.w, fmaf(w, dx, -er * dx), fx[k]);
                     fy[k] = fmaf(q.w, fmaf(w, dy, -er * dy), fy[k]);
@@ -650,19 +707,21 @@ KernelFn t3_kernel(const KParams &kp, int threads, int ipt, size_t *dyn_smem)
     return kp.order == 4 ? pick_t3<4>(threads, ipt) : pick_t3<2>(threads, ipt);
 }
 
-// z-row records of the haloed table: record (i, j, k) of the ext^3 grid holds
-// cells (i, j, k..k+3) as 3 float4, one per component (x taps, y taps, z taps).
-__global__ void k_table_zrow(const double *__restrict__ t, int ng, int halo, float4 *__restrict__ out)
+// Stencil records of the haloed table, 3 float4 per record (one per
+// component), record (i, j, k) of the ext^3 grid:
+//   tricubic: z row  -- cells (i, j, k..k+3)
+//   trilinear: (y, z) quad -- cells (i, j, k), (i, j, k+1), (i, j+1, k), (i, j+1, k+1)
+__global__ void k_table_records(const double *__restrict__ t, int ng, int halo, int order, float4 *__restrict__ out)
 {
     const int ext = ng + 2 * halo;
     const size_t ncell = (size_t)ext * ext * ext;
     size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= ncell) return;
     const int k = (int)(c % ext), j = (int)((c / ext) % ext), i = (int)(c / ((size_t)ext * ext));
-    const size_t row = ((size_t)pmod(i - halo, ng) * ng + pmod(j - halo, ng)) * ng;
     float v[3][4];
     for (int q = 0; q < 4; q++) {
-        const size_t s = row + pmod(k + q - halo, ng);
+        const int dj = order == 4 ? 0 : q >> 1, dk = order == 4 ? q : q & 1;
+        const size_t s = ((size_t)pmod(i - halo, ng) * ng + pmod(j + dj - halo, ng)) * ng + pmod(k + dk - halo, ng);
         for (int comp = 0; comp < 3; comp++) v[comp][q] = (float)t[3 * s + comp];
     }
     for (int comp = 0; comp < 3; comp++) out[3 * c + comp] = make_float4(v[comp][0], v[comp][1], v[comp][2], v[comp][3]);
@@ -687,17 +746,19 @@ const float4 *t3_table_f32(const Tables &tb, cudaStream_t st)
     return c.t3f.as<float4>();
 }
 
-// The z-row records for tricubic tables, rebuilt whenever the table changes.
-const float4 *t3_table_zrow(const Tables &tb, cudaStream_t st)
+// The stencil records for the table's interpolation order, rebuilt whenever
+// the table or the order changes.
+const float4 *t3_table_records(const Tables &tb, int order, cudaStream_t st)
 {
     Ctx &c = ctx();
     const size_t ext = (size_t)tb.t3_ng + 2 * T3_HALO;
     const size_t ncell = ext * ext * ext;
-    if (c.t3r_version != c.t3_version || !c.t3r.p) {
+    if (c.t3r_version != c.t3_version || c.t3r_order != order || !c.t3r.p) {
         float4 *o = c.t3r.ensure<float4>(3 * ncell);
-        k_table_zrow<<<(unsigned)((ncell + 255) / 256), 256, 0, st>>>(tb.t3, tb.t3_ng, T3_HALO, o);
-        note_launch("k_table_zrow");
+        k_table_records<<<(unsigned)((ncell + 255) / 256), 256, 0, st>>>(tb.t3, tb.t3_ng, T3_HALO, order, o);
+        note_launch("k_table_records");
         c.t3r_version = c.t3_version;
+        c.t3r_order = order;
     }
     return c.t3r.as<float4>();
 }
@@ -714,7 +775,7 @@ void t3_args(MixedArgs &a, const KParams &kp, const Tables &tb, cudaStream_t st)
     a.t3r = nullptr;
     if (kp.is_periodic >= 2) {
         a.t3f = t3_table_f32(tb, st);
-        if (kp.order == 4) a.t3r = t3_table_zrow(tb, st);
+        a.t3r = t3_table_records(tb, kp.order == 4 ? 4 : 2, st);
         a.ih = (float)((double)tb.t3_ng / kp.L);
         a.u0 = (float)((double)tb.t3_ng * 0.5 - 0.5);
     }
@@ -751,6 +812,10 @@ void s1tab_args(MixedArgs &a, const KParams &kp, const Tables &tb, cudaStream_t 
     a.irho = (float)(1.0 / drho);
     a.iz = (float)((double)tb.nz / kp.L);
     a.rho_max = (float)tb.rho_max;
+    a.s1_rho_max = tb.rho_max;
+    a.s1_idrho = drho > 0.0 ? 1.0 / drho : 0.0;
+    a.s1_idz = (double)tb.nz / kp.L;
+    a.s1_L = kp.L;
 }
 
 }  // namespace steps
