@@ -241,6 +241,13 @@ int steps_gpu_measure_peaks(double *fp32_flops, double *fp64_flops);
 /* Blocks until the library stream is idle; returns a pending kernel error. */
 int steps_gpu_synchronize(void);
 
+/* Page-locked host memory for the host-buffer calls (x, F of steps_gpu_forces,
+ * steps_gpu_upload_positions, ...): copies from and to it run at full DMA
+ * speed. The reference's driver arrays are ordinary malloc memory, which also
+ * works. *p is NULL on failure. */
+int steps_gpu_host_alloc(long long bytes, void **p);
+int steps_gpu_host_free(void *p);
+
 /* ---- allocation-free entry point ----------------------------------------- */
 
 /* No counterpart in the reference. Plain FP64 R^3 forces for callers that

@@ -103,11 +103,12 @@ class Engine:
         self._check(self.lib.steps_gpu_set_particles(int(m.size), _d(m), _d(eps)))
         self.n = int(m.size)
 
-    def forces(self, x, p: Params, precision=MIXED, id_min=0, id_max=None) -> np.ndarray:
+    def forces(self, x, p: Params, precision=MIXED, id_min=0, id_max=None, out=None) -> np.ndarray:
         x = np.ascontiguousarray(x, dtype=np.float64)
         if id_max is None:
             id_max = self.n - 1
-        F = np.empty((id_max - id_min + 1, 3))
+        F = np.empty((id_max - id_min + 1, 3)) if out is None else out
+        assert F.shape == (id_max - id_min + 1, 3) and F.dtype == np.float64 and F.flags.c_contiguous
         self._check(self.lib.steps_gpu_forces(C.byref(p), int(precision), _d(x), _d(F), int(id_min), int(id_max)))
         return F
 
@@ -234,6 +235,23 @@ class Engine:
 
     def flush_l2(self, nbytes: int = 512 << 20):
         self._check(self.lib.steps_gpu_flush_l2(int(nbytes)))
+
+    def host_array(self, shape):
+        """A float64 numpy array in page-locked host memory (freed with the
+        array's owner, this engine, at shutdown or via free_host_arrays)."""
+        n = int(np.prod(shape))
+        p = C.c_void_p()
+        self.lib.steps_gpu_host_alloc.argtypes = [C.c_longlong, C.POINTER(C.c_void_p)]
+        self._check(self.lib.steps_gpu_host_alloc(8 * max(n, 1), C.byref(p)))
+        self._pinned = getattr(self, "_pinned", []) + [p.value]
+        buf = (C.c_double * max(n, 1)).from_address(p.value)
+        return np.frombuffer(buf, dtype=np.float64, count=n).reshape(shape)
+
+    def free_host_arrays(self):
+        self.lib.steps_gpu_host_free.argtypes = [C.c_void_p]
+        for p in getattr(self, "_pinned", []):
+            self._check(self.lib.steps_gpu_host_free(C.c_void_p(p)))
+        self._pinned = []
 
     def synchronize(self):
         self._check(self.lib.steps_gpu_synchronize())

@@ -523,6 +523,27 @@ int steps_gpu_flush_l2(long long bytes)
     });
 }
 
+int steps_gpu_host_alloc(long long bytes, void **p)
+{
+    return guarded([&] {
+        if (!p || bytes <= 0) fail(STEPS_E_ARG, "host_alloc: positive size and a result pointer required");
+        *p = nullptr;
+        require_init();
+        if (cudaMallocHost(p, (size_t)bytes) != cudaSuccess) {
+            *p = nullptr;
+            cudaGetLastError();
+            fail(STEPS_E_NOMEM, "cudaMallocHost failed");
+        }
+    });
+}
+
+int steps_gpu_host_free(void *p)
+{
+    return guarded([&] {
+        if (p) STEPS_CUDA(cudaFreeHost(p));
+    });
+}
+
 int steps_gpu_synchronize(void)
 {
     return guarded([&] {

@@ -184,3 +184,21 @@ def test_errors(engine):
     assert e.value.code == S.STEPS_E_ARG
     # the context stays usable after errors
     assert rel_err(engine.forces(g["x"], S.params(S.R3), S.FP64), g["F"]).max() < FP64_TOL
+
+
+def test_page_locked_host_buffers(engine):
+    """steps_gpu_host_alloc memory works as the host buffers of the drop-in
+    call and gives bit-identical results to ordinary host memory."""
+    g = golden("r3_n2048")
+    engine.set_particles(g["m"], g["eps"])
+    x = engine.host_array(g["x"].shape)
+    x[...] = g["x"]
+    F = engine.host_array((2048, 3))
+    try:
+        engine.forces(x, S.params(S.R3), S.MIXED, out=F)
+        assert np.array_equal(F, engine.forces(g["x"], S.params(S.R3), S.MIXED))
+        engine.forces(x, S.params(S.R3), S.FP64, out=F)
+        assert rel_err(F, g["F"]).max() < 1e-12
+    finally:
+        del x, F
+        engine.free_host_arrays()
