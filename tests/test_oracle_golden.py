@@ -164,3 +164,37 @@ def test_r3_n32768_subset(port):
     lo, hi = (int(v) for v in g["r3_sub"])
     s = port.system(0, ps.m, ps.eps, port_params(O))
     assert rel_err(port.forces(s, ps.x, lo, hi), g["r3_F64"]).max() < TOL
+
+
+def test_s1r2_pair_line_mass_limit(port):
+    """Far from the axis (rho >> L) the singly periodic sum tends to a line of
+    mass m / L: radial force 2 m / (L rho), no z force. The oracle's pair force
+    and the reference's own values (golden probes with rho > 3 L, where the
+    first Fourier mode is down by exp(-2 pi rho / L) < 1e-8) both reach it."""
+    L = 200.0
+    alpha = 0.787875 / L
+    for rho in (2000.0, 4000.0):
+        for dz in (0.0, 37.0, -99.0):
+            F = port.s1r2_pair((0.6 * rho, 0.8 * rho, dz), L, alpha, 4, 10)
+            assert abs(math.hypot(F[0], F[1]) * L * rho / 2 - 1) < 1e-12
+            assert abs(F[2]) < 1e-20
+    g = golden("s1r2_table_o2")
+    probes, pair = g["probes"][: len(g["pair"])], g["pair"]
+    rho = np.hypot(probes[:, 0], probes[:, 1])
+    far = rho > 3 * float(g["L"])
+    assert far.sum() >= 3
+    radial = np.hypot(pair[far, 0], pair[far, 1]) * float(g["L"]) * rho[far] / 2
+    assert np.abs(radial - 1).max() < 1e-6
+
+
+def test_t3_table_odd_symmetry(port):
+    """The Ewald correction is odd, D(-r) = -D(r) (StePS/src/ewald_space.cc:365-376):
+    on the cell-centred grid cell i mirrors to ng - 1 - i. The reference's table
+    holds it exactly; so does the oracle's builder."""
+    g = golden("t3_o2")
+    ng = int(g["ngrid"])
+    T = g["table"].reshape(ng, ng, ng, 3)
+    assert np.abs(T + T[::-1, ::-1, ::-1]).max() == 0.0
+    e = [float(v) for v in g["ewald"]]
+    To = port.t3_table(ng, float(g["L"]), *e).reshape(ng, ng, ng, 3)
+    assert np.abs(To + To[::-1, ::-1, ::-1]).max() <= 1e-15 * np.abs(To).max()
