@@ -43,7 +43,7 @@ UNIT = "pairs/s"
 # Ewald table of the T^3 workload: Ng = 63, alpha = 2/L, real images |r+nL| <= 2L
 # (index radius 3), k vectors |k| <= 5 (2 pi / L) (index radius 6).
 T3_NG = 63
-LOOPS = ["fp32", "fp32x2", "fp32x2 (768 threads/SM)", "fp32x2 (1024 threads/SM)"]
+LOOPS = ["fp32", "fp32x2", "fp32x2 (768 threads/SM)", "fp32x2 (1024 threads/SM)", "fp32x2, bulk-copy mbarrier pipeline"]
 # DRAM bytes (read + write) of one launch of the pair kernel, from a one-pass ncu
 # capture of dram__bytes_read.sum + dram__bytes_write.sum (profiles/launches_r3_n1048576.md):
 # N = 2^20 R^3, 256x1 packed at 768 threads/SM, 64 j chunks.
@@ -70,7 +70,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--variant", type=int, default=-1,
-                    help="R^3 pair loop without autotuning: 0 fp32, 1 fp32x2, 2/3 fp32x2 at 768/1024 threads per SM")
+                    help="R^3 pair loop without autotuning: 0 fp32, 1 fp32x2, 2/3 fp32x2 at 768/1024 threads per SM, "
+                         "4 fp32x2 with the bulk-copy pipeline")
     ap.add_argument("--shape", default="", help="kernel shape THREADSxIPT without autotuning, e.g. 128x1")
     return ap.parse_args()
 

@@ -189,8 +189,11 @@ int steps_gpu_batch_get(int k, double *x, double *v, double *F);
 int steps_gpu_set_tuning(int threads, int ipt, int jsplit);
 
 /* R^3 mixed-precision pair loop: 0 = scalar FP32 instructions, 1 = packed
- * FP32x2 instructions (two pairs per instruction, sm_100+). Same results to
- * rounding; the autotuner picks between them. */
+ * FP32x2 instructions (two pairs per instruction, sm_100+), 2 / 3 = packed
+ * with 768 / 1024 resident threads per SM asked of the register allocator,
+ * 4 = packed with the j tiles streamed by bulk copies (TMA) through an
+ * mbarrier ring (bounded waits; STEPS_E_TIMEOUT if one gives up). Same results
+ * to rounding; the autotuner picks among them. */
 int steps_gpu_set_kernel_variant(int variant);
 
 /* T^3 mixed precision: capacity, in table cells (16 bytes each), of the

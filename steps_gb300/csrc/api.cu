@@ -217,8 +217,10 @@ int steps_gpu_shutdown(void)
         cudaStreamSynchronize(c.stream);
         batch_release();
         DevBuf *bufs[] = {&c.m64, &c.eps64, &c.x, &c.v, &c.F, &c.pack64, &c.partial, &c.bbox, &c.counter,
-                          &c.status, &c.flush, &c.peaks, &c.t3, &c.t3f, &c.s1r2, &c.s1f, &c.radial};
+                          &c.status, &c.flush, &c.peaks, &c.t3, &c.t3f, &c.t3r, &c.s1r2, &c.s1f, &c.s1rec,
+                          &c.radial, &c.kstatus};
         for (DevBuf *b : bufs) b->release();
+        if (c.kstatus_host) cudaFreeHost(c.kstatus_host);
         TileSet *ts[] = {&c.tj, &c.ti};
         for (TileSet *t : ts) {
             for (int k = 0; k < 2; k++) { t->keys[k].release(); t->vals[k].release(); }
@@ -429,12 +431,13 @@ int steps_gpu_autotune(const steps_params *p, int id_min, int id_max, int *out)
         Shape bestS = keep;
         KParams kp = derive_params(p);
         // R^3: the scalar and packed pair loops as well.
-        const int nvar = kp.topology == STEPS_R3 ? 4 : 1;
+        const int nvar = kp.topology == STEPS_R3 ? R3_VARIANTS : 1;
         compute_forces(p, STEPS_MIXED, id_min, id_max, false);  // orders the particles, loads modules
         for (int v = 0; v < nvar; v++)
             for (auto &s : shapes) {
                 if (!shape_supported_for(kp, s[0], s[1])) continue;
-                if (v >= 1 && !r3x2_kernel(s[0], s[1], false, r3x2_occ(v))) continue;
+                if (v >= 1 && v <= 3 && !r3x2_kernel(s[0], s[1], false, r3x2_occ(v))) continue;
+                if (v == 4 && !r3x2_pipe_kernel(s[0], s[1])) continue;
                 c.shape.threads = s[0];
                 c.shape.ipt = s[1];
                 c.shape.jsplit = 0;
@@ -472,9 +475,9 @@ int steps_gpu_set_t3_window(int cells)
 int steps_gpu_set_kernel_variant(int variant)
 {
     return guarded([&] {
-        if (variant < 0 || variant > 3)
+        if (variant < 0 || variant >= R3_VARIANTS)
             fail(STEPS_E_ARG, "kernel variant must be 0 (scalar), 1 (packed FP32x2), 2 or 3 (packed, 768 or 1024 "
-                              "threads per SM)");
+                              "threads per SM) or 4 (packed, bulk-copy pipeline)");
         g_ctx.shape.variant = variant;
     });
 }

@@ -85,7 +85,8 @@ struct Shape {
     int threads = 128;
     int ipt = 2;
     int jsplit = 0;
-    int variant = 0;  // R^3: 0 scalar FP32 pair loop; 1, 2, 3 packed FP32x2 (0, 768, 1024 threads/SM asked)
+    int variant = 0;  // R^3: 0 scalar FP32 pair loop; 1, 2, 3 packed FP32x2 (0, 768, 1024 threads/SM
+                      // asked); 4 packed with the bulk-copy (TMA) + mbarrier pipeline
     float guard = 30.0f;  // tile-pair scale / gap above which the double-float path runs
     int t3_cells = 0;  // T^3: shared-memory table window capacity in cells (0 = haloed table via L1/L2)
 };

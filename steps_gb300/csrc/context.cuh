@@ -27,6 +27,8 @@ struct Ctx {
     DevBuf pack64;                   // FP64 kernel j stream: (x, y, z, m) per particle
     DevBuf partial;                  // per-j-chunk partial forces (FP64)
     DevBuf bbox, counter, status, flush, peaks;
+    DevBuf kstatus;                  // int written by kernels whose bounded waits give up
+    int *kstatus_host = nullptr;     // page-locked mirror of kstatus
     TileSet tj, ti;                  // j set (all particles) and i subset tiles
 
     DevBuf t3;

@@ -26,6 +26,7 @@ struct MixedArgs {
     int S, tpc;  // j chunks per i tile, j tiles per chunk
     int nitems;
     unsigned *counter;
+    int *status;        // STEPS_E_TIMEOUT written here by a pipeline wait that gave up
     const int4 *items;  // work list (batches): i tile, j tile begin, j tile end, partial slot
     double *part;       // [S][nit*T][3]
     size_t part_stride; // nit*T*3
@@ -244,6 +245,58 @@ __device__ __forceinline__ f2 f2_fma(f2 a, f2 b, f2 c)
     return r;
 }
 
+// ---- mbarrier + bulk-copy (TMA) pipeline helpers -------------------------
+
+// SM clock cycles a bounded mbarrier wait lasts before the kernel gives up,
+// records STEPS_E_TIMEOUT and returns (about a second; a healthy wait in these
+// kernels takes microseconds).
+constexpr long long MBAR_WAIT_CYCLES = 2000000000LL;
+
+__device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void mbar_arrive(unsigned long long *bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long *bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity)
+{
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Waits for the phase with the given parity to complete; false after
+// MBAR_WAIT_CYCLES (the caller records the error and leaves).
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity)
+{
+    if (mbar_try_wait(bar, parity)) return true;
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity))
+        if (clock64() - t0 > MBAR_WAIT_CYCLES) return false;
+    return true;
+}
+// Bulk copy global -> shared of `bytes` (multiple of 16, both addresses
+// 16-byte aligned), completion counted on the mbarrier as transaction bytes.
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, unsigned long long *bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+
 using KernelFn = void (*)(MixedArgs);
 
 }  // namespace mixed
@@ -257,6 +310,10 @@ void t3_args(mixed::MixedArgs &a, const KParams &kp, const Tables &tb, cudaStrea
 mixed::KernelFn r3x2_kernel(int threads, int ipt, bool list = false, int occ = 0);
 // Resident-thread request of a packed R^3 kernel variant (1, 2, 3).
 inline int r3x2_occ(int variant) { return variant == 2 ? 768 : variant == 3 ? 1024 : 0; }
+// pair_r3x2.cu: the packed R^3 kernel with its j tiles streamed by bulk
+// copies through an mbarrier ring (variant 4).
+mixed::KernelFn r3x2_pipe_kernel(int threads, int ipt);
+constexpr int R3_VARIANTS = 5;  // 0 scalar, 1-3 packed, 4 packed + bulk-copy pipeline
 // S1xR2 with the (rho, z) table (IS_PERIODIC >= 2, no explicit images).
 mixed::KernelFn s1tab_kernel(const KParams &kp, int threads, int ipt);
 void s1tab_args(mixed::MixedArgs &a, const KParams &kp, const Tables &tb, cudaStream_t st);

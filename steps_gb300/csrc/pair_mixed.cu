@@ -401,7 +401,8 @@ void forces_mixed(const KParams &kp, const Tables &tb, const double *x, const do
     const bool packed = kp.topology == STEPS_R3 && c.shape.variant >= 1;
     KernelFn fn = kp.topology == STEPS_T3 ? t3_kernel(kp, threads, ipt, &dyn)
                   : s1tab              ? s1tab_kernel(kp, threads, ipt)
-                  : packed             ? r3x2_kernel(threads, ipt, false, r3x2_occ(c.shape.variant))
+                  : packed             ? (c.shape.variant == 4 ? r3x2_pipe_kernel(threads, ipt)
+                                                               : r3x2_kernel(threads, ipt, false, r3x2_occ(c.shape.variant)))
                                        : select_kernel(kp, threads, ipt);
     if (!fn) fail(STEPS_E_ARG, "mixed precision: unsupported topology/mode or kernel shape");
 
@@ -488,10 +489,20 @@ void forces_mixed(const KParams &kp, const Tables &tb, const double *x, const do
     if (kp.topology == STEPS_T3) t3_args(a, kp, tb, st);
     if (s1tab) s1tab_args(a, kp, tb, st);
 
+    a.status = c.kstatus.ensure<int>(1);
     STEPS_CUDA(cudaMemsetAsync(a.counter, 0, sizeof(unsigned), st));
+    const bool bounded_waits = packed && c.shape.variant == 4;
+    if (bounded_waits) STEPS_CUDA(cudaMemsetAsync(a.status, 0, sizeof(int), st));
     int grid = resident < a.nitems ? resident : a.nitems;
     fn<<<grid, threads, dyn, st>>>(a);
     note_launch("k_pair_mixed");
+    if (bounded_waits) {
+        // A kernel whose bounded waits gave up has left and written its status.
+        if (!c.kstatus_host) STEPS_CUDA(cudaMallocHost(&c.kstatus_host, sizeof(int)));
+        STEPS_CUDA(cudaMemcpyAsync(c.kstatus_host, a.status, sizeof(int), cudaMemcpyDeviceToHost, st));
+        STEPS_CUDA(cudaStreamSynchronize(st));
+        if (*c.kstatus_host != 0) fail(STEPS_E_TIMEOUT, "pair kernel: a pipeline wait timed out (status written by the kernel)");
+    }
     STEPS_CUDA(cudaEventRecord(c.phase[2], st));
     k_reduce_mixed<<<div_up(ni, 256), 256, 0, st>>>(a.part, S, a.part_stride, ti.perm(), ni, id_min, x,
                                                    background_of(kp, tb), F);

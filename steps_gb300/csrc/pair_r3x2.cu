@@ -40,6 +40,114 @@ __device__ __forceinline__ void stage_soa(const MixedArgs &a, int J, float *sx, 
     cp_commit();
 }
 
+// One j tile J against this thread's i particles: the staged tile is sxb
+// (X[T], Y[T], Z[T], M[T]), seb (softening), sidb (ids), sresb (residuals).
+template <int BLOCK, int IPT>
+__device__ __forceinline__ void r3x2_tile(const MixedArgs &a, int J, const float *sxb, const float *seb,
+                                          const uint32_t *sidb, const float4 *sresb, float4 mI0, float4 wc, float4 wh,
+                                          const float *xi, const float *yi, const float *zi, const float *ei,
+                                          const float *lx, const float *ly, const float *lz, const uint32_t *ii,
+                                          double *ax, double *ay, double *az)
+{
+    constexpr int T = BLOCK * IPT;
+    const float4 mJ0 = __ldg(a.jmeta + 2 * J);
+    const float4 mJ1 = __ldg(a.jmeta + 2 * J + 1);
+    float eOx, eOy, eOz;
+    const float dOx = two_diff(mJ0.x, mI0.x, eOx), dOy = two_diff(mJ0.y, mI0.y, eOy),
+                dOz = two_diff(mJ0.z, mI0.z, eOz);
+    // Near field / coarse FP32 scale, decided per warp (warp-uniform
+    // branch): in a near tile pair, warps away from J keep the far loop.
+    const bool full = warp_full(dOx, dOy, dOz, wc, wh, mJ1, mI0.w + mJ0.w, a.guard2);
+    const float *X = sxb;
+    const float *Y = X + T;
+    const float *Z = X + 2 * T;
+    const float *Mq = X + 3 * T;
+
+    if (!full) {
+        f2 PX[IPT], PY[IPT], PZ[IPT], AX[IPT], AY[IPT], AZ[IPT];
+#pragma unroll
+        for (int k = 0; k < IPT; k++) {
+            PX[k] = f2_bcast(((xi[k] - dOx) - eOx) + lx[k]);
+            PY[k] = f2_bcast(((yi[k] - dOy) - eOy) + ly[k]);
+            PZ[k] = f2_bcast(((zi[k] - dOz) - eOz) + lz[k]);
+            AX[k] = AY[k] = AZ[k] = 0ull;  // {+0, +0}
+        }
+#pragma unroll 2
+        for (int jj = 0; jj < T; jj += 4) {
+            const ulonglong2 qx4 = *reinterpret_cast<const ulonglong2 *>(X + jj);
+            const ulonglong2 qy4 = *reinterpret_cast<const ulonglong2 *>(Y + jj);
+            const ulonglong2 qz4 = *reinterpret_cast<const ulonglong2 *>(Z + jj);
+            const ulonglong2 qm4 = *reinterpret_cast<const ulonglong2 *>(Mq + jj);
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const f2 qx = h ? qx4.y : qx4.x, qy = h ? qy4.y : qy4.x, qz = h ? qz4.y : qz4.x;
+                const f2 qm = h ? qm4.y : qm4.x;
+#pragma unroll
+                for (int k = 0; k < IPT; k++) {
+                    const f2 dx = f2_sub(qx, PX[k]), dy = f2_sub(qy, PY[k]), dz = f2_sub(qz, PZ[k]);
+                    const f2 r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx)));
+                    float r2a, r2b;
+                    f2_unpack(r2, r2a, r2b);
+                    const f2 ri = f2_pack(rsqrt_mufu(r2a), rsqrt_mufu(r2b));
+                    const f2 w = f2_mul(f2_mul(qm, ri), f2_mul(ri, ri));
+                    AX[k] = f2_fma(w, dx, AX[k]);
+                    AY[k] = f2_fma(w, dy, AY[k]);
+                    AZ[k] = f2_fma(w, dz, AZ[k]);
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < IPT; k++) {
+            float l0, l1;
+            f2_unpack(AX[k], l0, l1);
+            ax[k] += (double)(l0 + l1);
+            f2_unpack(AY[k], l0, l1);
+            ay[k] += (double)(l0 + l1);
+            f2_unpack(AZ[k], l0, l1);
+            az[k] += (double)(l0 + l1);
+        }
+    } else {
+        // Near field: scalar double-float path with the spline
+        // (StePS/src/forces.cc:52-87); the self pair gets d = 0.
+        float phx[IPT], phy[IPT], phz[IPT], plx[IPT], ply[IPT], plz[IPT], fx[IPT], fy[IPT], fz[IPT];
+#pragma unroll
+        for (int k = 0; k < IPT; k++) {
+            frame_split(xi[k], lx[k], dOx, eOx, phx[k], plx[k]);
+            frame_split(yi[k], ly[k], dOy, eOy, phy[k], ply[k]);
+            frame_split(zi[k], lz[k], dOz, eOz, phz[k], plz[k]);
+            fx[k] = fy[k] = fz[k] = 0.0f;
+        }
+        for (int jj = 0; jj < T; ++jj) {
+            const float qx = X[jj], qy = Y[jj], qz = Z[jj], qm = Mq[jj];
+            const float ej = seb[jj];
+            const uint32_t jid = sidb[jj];
+            const float4 ql = sresb[jj];
+#pragma unroll
+            for (int k = 0; k < IPT; k++) {
+                const bool self = jid == ii[k];
+                const float dx = self ? 0.0f : (qx - phx[k]) + (ql.x - plx[k]);
+                const float dy = self ? 0.0f : (qy - phy[k]) + (ql.y - ply[k]);
+                const float dz = self ? 0.0f : (qz - phz[k]) + (ql.z - plz[k]);
+                const float b = ei[k] + ej;
+                const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                const float ri = rsqrt_mufu(r2);
+                float w = ri * ri * ri;
+                if (r2 < b * b) w = spline_inner_f32(r2, b);
+                w *= qm;
+                fx[k] = fmaf(w, dx, fx[k]);
+                fy[k] = fmaf(w, dy, fy[k]);
+                fz[k] = fmaf(w, dz, fz[k]);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < IPT; k++) {
+            ax[k] += (double)fx[k];
+            ay[k] += (double)fy[k];
+            az[k] += (double)fz[k];
+        }
+    }
+}
+
 template <int BLOCK, int IPT, bool LIST>
 __device__ __forceinline__ void r3x2_body(const MixedArgs &a)
 {
@@ -108,105 +216,8 @@ __device__ __forceinline__ void r3x2_body(const MixedArgs &a)
             }
             __syncthreads();
 
-            const float4 mJ0 = __ldg(a.jmeta + 2 * J);
-            const float4 mJ1 = __ldg(a.jmeta + 2 * J + 1);
-            float eOx, eOy, eOz;
-            const float dOx = two_diff(mJ0.x, mI0.x, eOx), dOy = two_diff(mJ0.y, mI0.y, eOy),
-                        dOz = two_diff(mJ0.z, mI0.z, eOz);
-            // Near field / coarse FP32 scale, decided per warp (warp-uniform
-            // branch): in a near tile pair, warps away from J keep the far loop.
-            const bool full = warp_full(dOx, dOy, dOz, wc, wh, mJ1, mI0.w + mJ0.w, a.guard2);
-            const float *X = sx[buf];
-            const float *Y = X + T;
-            const float *Z = X + 2 * T;
-            const float *Mq = X + 3 * T;
-
-            if (!full) {
-                f2 PX[IPT], PY[IPT], PZ[IPT], AX[IPT], AY[IPT], AZ[IPT];
-#pragma unroll
-                for (int k = 0; k < IPT; k++) {
-                    PX[k] = f2_bcast(((xi[k] - dOx) - eOx) + lx[k]);
-                    PY[k] = f2_bcast(((yi[k] - dOy) - eOy) + ly[k]);
-                    PZ[k] = f2_bcast(((zi[k] - dOz) - eOz) + lz[k]);
-                    AX[k] = AY[k] = AZ[k] = 0ull;  // {+0, +0}
-                }
-#pragma unroll 2
-                for (int jj = 0; jj < T; jj += 4) {
-                    const ulonglong2 qx4 = *reinterpret_cast<const ulonglong2 *>(X + jj);
-                    const ulonglong2 qy4 = *reinterpret_cast<const ulonglong2 *>(Y + jj);
-                    const ulonglong2 qz4 = *reinterpret_cast<const ulonglong2 *>(Z + jj);
-                    const ulonglong2 qm4 = *reinterpret_cast<const ulonglong2 *>(Mq + jj);
-#pragma unroll
-                    for (int h = 0; h < 2; h++) {
-                        const f2 qx = h ? qx4.y : qx4.x, qy = h ? qy4.y : qy4.x, qz = h ? qz4.y : qz4.x;
-                        const f2 qm = h ? qm4.y : qm4.x;
-#pragma unroll
-                        for (int k = 0; k < IPT; k++) {
-                            const f2 dx = f2_sub(qx, PX[k]), dy = f2_sub(qy, PY[k]), dz = f2_sub(qz, PZ[k]);
-                            const f2 r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx)));
-                            float r2a, r2b;
-                            f2_unpack(r2, r2a, r2b);
-                            const f2 ri = f2_pack(rsqrt_mufu(r2a), rsqrt_mufu(r2b));
-                            const f2 w = f2_mul(f2_mul(qm, ri), f2_mul(ri, ri));
-                            AX[k] = f2_fma(w, dx, AX[k]);
-                            AY[k] = f2_fma(w, dy, AY[k]);
-                            AZ[k] = f2_fma(w, dz, AZ[k]);
-                        }
-                    }
-                }
-#pragma unroll
-                for (int k = 0; k < IPT; k++) {
-                    float l0, l1;
-                    f2_unpack(AX[k], l0, l1);
-                    ax[k] += (double)(l0 + l1);
-                    f2_unpack(AY[k], l0, l1);
-                    ay[k] += (double)(l0 + l1);
-                    f2_unpack(AZ[k], l0, l1);
-                    az[k] += (double)(l0 + l1);
-                }
-            } else {
-                // Near field: scalar double-float path with the spline
-                // (StePS/src/forces.cc:52-87); the self pair gets d = 0.
-                float phx[IPT], phy[IPT], phz[IPT], plx[IPT], ply[IPT], plz[IPT], fx[IPT], fy[IPT], fz[IPT];
-#pragma unroll
-                for (int k = 0; k < IPT; k++) {
-                    frame_split(xi[k], lx[k], dOx, eOx, phx[k], plx[k]);
-                    frame_split(yi[k], ly[k], dOy, eOy, phy[k], ply[k]);
-                    frame_split(zi[k], lz[k], dOz, eOz, phz[k], plz[k]);
-                    fx[k] = fy[k] = fz[k] = 0.0f;
-                }
-                const float *seb = se[buf];
-                const uint32_t *sidb = sid[buf];
-                const float4 *sresb = sres[buf];
-                for (int jj = 0; jj < T; ++jj) {
-                    const float qx = X[jj], qy = Y[jj], qz = Z[jj], qm = Mq[jj];
-                    const float ej = seb[jj];
-                    const uint32_t jid = sidb[jj];
-                    const float4 ql = sresb[jj];
-#pragma unroll
-                    for (int k = 0; k < IPT; k++) {
-                        const bool self = jid == ii[k];
-                        const float dx = self ? 0.0f : (qx - phx[k]) + (ql.x - plx[k]);
-                        const float dy = self ? 0.0f : (qy - phy[k]) + (ql.y - ply[k]);
-                        const float dz = self ? 0.0f : (qz - phz[k]) + (ql.z - plz[k]);
-                        const float b = ei[k] + ej;
-                        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                        const float ri = rsqrt_mufu(r2);
-                        float w = ri * ri * ri;
-                        if (r2 < b * b) w = spline_inner_f32(r2, b);
-                        w *= qm;
-                        fx[k] = fmaf(w, dx, fx[k]);
-                        fy[k] = fmaf(w, dy, fy[k]);
-                        fz[k] = fmaf(w, dz, fz[k]);
-                    }
-                }
-#pragma unroll
-                for (int k = 0; k < IPT; k++) {
-                    ax[k] += (double)fx[k];
-                    ay[k] += (double)fy[k];
-                    az[k] += (double)fz[k];
-                }
-            }
+            r3x2_tile<BLOCK, IPT>(a, J, sx[buf], se[buf], sid[buf], sres[buf], mI0, wc, wh, xi, yi, zi, ei, lx, ly, lz,
+                                  ii, ax, ay, az);
             __syncthreads();
         }
 
@@ -219,6 +230,132 @@ __device__ __forceinline__ void r3x2_body(const MixedArgs &a)
             o[3 * e + 2] = az[k];
         }
     }
+}
+
+// The same work as r3x2_body with the j tiles streamed through an S-stage
+// shared-memory ring filled by bulk copies (cp.async.bulk, the TMA engine)
+// and tracked by mbarriers: full[s] completes when stage s has landed,
+// empty[s] when every warp has finished with it. Thread 0 issues the copy of
+// tile J + S - 1 when it starts tile J, so warps wait only for their data,
+// never for each other, and drift up to S - 1 tiles apart (no block-wide
+// barrier per tile). Every wait is bounded: a wait that gives up writes
+// STEPS_E_TIMEOUT to a.status, the block stops taking work, and thread 0
+// waits (bounded) for its copies in flight before the block exits.
+template <int BLOCK, int IPT>
+__device__ __forceinline__ void r3x2_pipe_body(const MixedArgs &a)
+{
+    constexpr int T = BLOCK * IPT;
+    constexpr int S = T <= 256 ? 4 : 2;
+    constexpr int NW = BLOCK / 32;
+    constexpr unsigned BYTES = 40u * T;  // SoA 16T + softening 4T + ids 4T + residuals 16T
+    __shared__ __align__(128) float sx[S][4 * T];  // per stage X[T], Y[T], Z[T], M[T]
+    __shared__ __align__(16) float se[S][T];
+    __shared__ __align__(16) uint32_t sid[S][T];
+    __shared__ __align__(16) float4 sres[S][T];
+    __shared__ __align__(8) unsigned long long full[S], empty[S];
+    __shared__ int s_item, s_abort;
+    const int tid = threadIdx.x, lane = tid & 31;
+    if (tid == 0) {
+        for (int st = 0; st < S; st++) {
+            mbar_init(&full[st], 1);
+            mbar_init(&empty[st], NW);
+        }
+        mbar_fence_init();
+        s_abort = 0;
+    }
+    __syncthreads();
+    unsigned long long issued = 0;    // tiles whose copy thread 0 has issued
+    unsigned long long consumed = 0;  // tiles this thread's warp has finished (the same in every warp)
+    auto issue = [&](int J) -> bool {  // thread 0
+        const int st = (int)(issued % S);
+        if (issued >= S && !mbar_wait(&empty[st], (unsigned)((issued / S - 1) & 1))) return false;
+        mbar_arrive_expect_tx(&full[st], BYTES);
+        bulk_g2s(sx[st], a.jsoa + (size_t)J * 4 * T, 16u * T, &full[st]);
+        bulk_g2s(se[st], a.jeps + (size_t)J * T, 4u * T, &full[st]);
+        bulk_g2s(sid[st], a.jidx + (size_t)J * T, 4u * T, &full[st]);
+        bulk_g2s(sres[st], a.jres + (size_t)J * T, 16u * T, &full[st]);
+        issued++;
+        return true;
+    };
+    auto abort_block = [&]() {
+        s_abort = 1;
+        atomicExch(a.status, STEPS_E_TIMEOUT);
+    };
+
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) s_item = s_abort ? a.nitems : (int)atomicAdd(a.counter, 1u);
+        __syncthreads();
+        const int item = s_item;
+        if (item >= a.nitems) break;
+        const int I = item / a.S;
+        const int chunk = item - I * a.S;
+        const int J0 = chunk * a.tpc;
+        const int J1 = min(a.njt, J0 + a.tpc);
+        const size_t base = (size_t)chunk * a.part_stride + 3 * (size_t)I * T;
+
+        const float4 mI0 = __ldg(a.imeta + 2 * I);
+        float xi[IPT], yi[IPT], zi[IPT], ei[IPT], lx[IPT], ly[IPT], lz[IPT];
+        uint32_t ii[IPT];
+        double ax[IPT], ay[IPT], az[IPT];
+#pragma unroll
+        for (int k = 0; k < IPT; k++) {
+            const size_t q = (size_t)I * T + k * BLOCK + tid;
+            const float4 p = __ldg(a.ipack + q);
+            xi[k] = p.x;
+            yi[k] = p.y;
+            zi[k] = p.z;
+            ei[k] = __ldg(a.ieps + q);
+            ii[k] = __ldg(a.iidx + q);
+            const float4 l = __ldg(a.ilo + q);
+            lx[k] = l.x;
+            ly[k] = l.y;
+            lz[k] = l.z;
+            ax[k] = ay[k] = az[k] = 0.0;
+        }
+        float4 wc, wh;
+        warp_box<IPT>(xi, yi, zi, wc, wh);
+
+        bool ok = true;
+        if (tid == 0)
+            for (int J = J0; J < J1 && J < J0 + S - 1 && ok; J++) ok = issue(J);
+        for (int J = J0; J < J1; ++J) {
+            bool mine = true;
+            if (tid == 0 && ok && J + S - 1 < J1) mine = ok = issue(J + S - 1);
+            if (tid == 0 && !ok) mine = false;
+            const int st = (int)(consumed % S);
+            mine = mine && mbar_wait(&full[st], (unsigned)((consumed / S) & 1));
+            if (!__all_sync(0xffffffffu, mine)) {  // warp-uniform
+                if (lane == 0) abort_block();
+                break;
+            }
+            r3x2_tile<BLOCK, IPT>(a, J, sx[st], se[st], sid[st], sres[st], mI0, wc, wh, xi, yi, zi, ei, lx, ly, lz, ii,
+                                  ax, ay, az);
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&empty[st]);
+            consumed++;
+        }
+
+        double *o = a.part + base;
+#pragma unroll
+        for (int k = 0; k < IPT; k++) {
+            const size_t e = k * BLOCK + tid;
+            o[3 * e] = ax[k];
+            o[3 * e + 1] = ay[k];
+            o[3 * e + 2] = az[k];
+        }
+    }
+    // After an abort, copies may still be in flight into this block's shared
+    // memory: thread 0 waits for them (bounded) before the block exits.
+    if (tid == 0)
+        for (unsigned long long q = consumed; q < issued; q++)
+            if (!mbar_wait(&full[q % S], (unsigned)((q / S) & 1))) break;
+}
+
+template <int BLOCK, int IPT>
+__global__ void __launch_bounds__(BLOCK) k_pair_r3x2_pipe(MixedArgs a)
+{
+    r3x2_pipe_body<BLOCK, IPT>(a);
 }
 
 template <int BLOCK, int IPT, bool LIST>
@@ -237,6 +374,17 @@ __global__ void __launch_bounds__(BLOCK, OCC / BLOCK) k_pair_r3x2_occ(MixedArgs 
 }
 
 }  // namespace
+
+KernelFn r3x2_pipe_kernel(int threads, int ipt)
+{
+#define STEPS_SHAPE(B, P) \
+    if (threads == B && ipt == P) return k_pair_r3x2_pipe<B, P>;
+    STEPS_SHAPE(64, 1) STEPS_SHAPE(64, 2) STEPS_SHAPE(64, 4)
+    STEPS_SHAPE(128, 1) STEPS_SHAPE(128, 2) STEPS_SHAPE(128, 4)
+    STEPS_SHAPE(256, 1) STEPS_SHAPE(256, 2)
+#undef STEPS_SHAPE
+    return nullptr;
+}
 
 KernelFn r3x2_kernel(int threads, int ipt, bool list, int occ)
 {

@@ -118,11 +118,11 @@ def test_shapes_agree(engine, port):
 
 def test_packed_fp32x2_variant(engine, port):
     """The packed FP32x2 pair loop agrees with the reference like the scalar one,
-    at each register budget (variants 1-3)."""
+    at each register budget (variants 1-3) and with the bulk-copy pipeline (4)."""
     g = golden("r3_n2048")
     engine.set_particles(g["m"], g["eps"])
     try:
-        for variant in (1, 2, 3):
+        for variant in (1, 2, 3, 4):
             engine.set_variant(variant)
             for threads, ipt in ((64, 1), (64, 2), (64, 4), (128, 1), (128, 2), (128, 4), (256, 1), (256, 2)):
                 engine.set_tuning(threads, ipt, 0)
