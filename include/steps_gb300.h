@@ -251,6 +251,14 @@ int steps_gpu_synchronize(void);
 int steps_gpu_host_alloc(long long bytes, void **p);
 int steps_gpu_host_free(void *p);
 
+/* Test hook for the bounded waits (no counterpart in the reference): in the
+ * next mixed R^3 force evaluation with pair-loop variant 4, block 0 withholds
+ * the bulk copy of its tile number tile_seq (0-based, counted over the block's
+ * work), so the waits on that tile run out after about a second. The call then
+ * returns STEPS_E_TIMEOUT, the kernel having left cleanly, and the context
+ * stays usable. -1 cancels. One shot. */
+int steps_gpu_test_stall_copy(long long tile_seq);
+
 /* ---- allocation-free entry point ----------------------------------------- */
 
 /* No counterpart in the reference. Plain FP64 R^3 forces for callers that

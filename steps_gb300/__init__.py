@@ -218,6 +218,10 @@ class Engine:
     def set_t3_window(self, cells: int):
         self._check(self.lib.steps_gpu_set_t3_window(int(cells)))
 
+    def test_stall_copy(self, tile_seq: int):
+        self.lib.steps_gpu_test_stall_copy.argtypes = [C.c_longlong]
+        self._check(self.lib.steps_gpu_test_stall_copy(int(tile_seq)))
+
     def set_variant(self, variant: int):
         self._check(self.lib.steps_gpu_set_kernel_variant(int(variant)))
 

@@ -526,6 +526,14 @@ int steps_gpu_flush_l2(long long bytes)
     });
 }
 
+int steps_gpu_test_stall_copy(long long tile_seq)
+{
+    return guarded([&] {
+        if (tile_seq < -1) fail(STEPS_E_ARG, "tile_seq must be >= -1");
+        g_ctx.stall_seq = tile_seq;
+    });
+}
+
 int steps_gpu_host_alloc(long long bytes, void **p)
 {
     return guarded([&] {

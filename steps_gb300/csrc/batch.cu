@@ -192,6 +192,7 @@ void batch_forces(Batch &b)
                      PAD_J, b.ts.resid.as<float4>(), b.ts.soa.as<float>(), b.tdesc.as<int2>(), b.ntiles, st);
 
     mixed::MixedArgs a{};
+    a.stall_seq = -1;
     a.jpack = a.ipack = b.ts.pack.as<float4>();
     a.jeps = a.ieps = b.ts.eps.as<float>();
     a.jmeta = a.imeta = b.ts.meta.as<float4>();

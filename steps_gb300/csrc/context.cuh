@@ -29,6 +29,7 @@ struct Ctx {
     DevBuf bbox, counter, status, flush, peaks;
     DevBuf kstatus;                  // int written by kernels whose bounded waits give up
     int *kstatus_host = nullptr;     // page-locked mirror of kstatus
+    long long stall_seq = -1;        // test hook for the next pipelined launch (one shot)
     TileSet tj, ti;                  // j set (all particles) and i subset tiles
 
     DevBuf t3;

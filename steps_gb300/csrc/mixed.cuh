@@ -27,6 +27,7 @@ struct MixedArgs {
     int nitems;
     unsigned *counter;
     int *status;        // STEPS_E_TIMEOUT written here by a pipeline wait that gave up
+    long long stall_seq;  // test hook: block 0 withholds the copy of its tile number stall_seq (-1: none)
     const int4 *items;  // work list (batches): i tile, j tile begin, j tile end, partial slot
     double *part;       // [S][nit*T][3]
     size_t part_stride; // nit*T*3

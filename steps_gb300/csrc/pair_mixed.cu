@@ -490,6 +490,8 @@ void forces_mixed(const KParams &kp, const Tables &tb, const double *x, const do
     if (s1tab) s1tab_args(a, kp, tb, st);
 
     a.status = c.kstatus.ensure<int>(1);
+    a.stall_seq = c.stall_seq;
+    c.stall_seq = -1;
     STEPS_CUDA(cudaMemsetAsync(a.counter, 0, sizeof(unsigned), st));
     const bool bounded_waits = packed && c.shape.variant == 4;
     if (bounded_waits) STEPS_CUDA(cudaMemsetAsync(a.status, 0, sizeof(int), st));

@@ -270,10 +270,13 @@ __device__ __forceinline__ void r3x2_pipe_body(const MixedArgs &a)
         const int st = (int)(issued % S);
         if (issued >= S && !mbar_wait(&empty[st], (unsigned)((issued / S - 1) & 1))) return false;
         mbar_arrive_expect_tx(&full[st], BYTES);
-        bulk_g2s(sx[st], a.jsoa + (size_t)J * 4 * T, 16u * T, &full[st]);
-        bulk_g2s(se[st], a.jeps + (size_t)J * T, 4u * T, &full[st]);
-        bulk_g2s(sid[st], a.jidx + (size_t)J * T, 4u * T, &full[st]);
-        bulk_g2s(sres[st], a.jres + (size_t)J * T, 16u * T, &full[st]);
+        // test hook: withhold one copy so that the waits on it run out
+        if (!(blockIdx.x == 0 && (long long)issued == a.stall_seq)) {
+            bulk_g2s(sx[st], a.jsoa + (size_t)J * 4 * T, 16u * T, &full[st]);
+            bulk_g2s(se[st], a.jeps + (size_t)J * T, 4u * T, &full[st]);
+            bulk_g2s(sid[st], a.jidx + (size_t)J * T, 4u * T, &full[st]);
+            bulk_g2s(sres[st], a.jres + (size_t)J * T, 16u * T, &full[st]);
+        }
         issued++;
         return true;
     };
@@ -348,8 +351,7 @@ __device__ __forceinline__ void r3x2_pipe_body(const MixedArgs &a)
     // After an abort, copies may still be in flight into this block's shared
     // memory: thread 0 waits for them (bounded) before the block exits.
     if (tid == 0)
-        for (unsigned long long q = consumed; q < issued; q++)
-            if (!mbar_wait(&full[q % S], (unsigned)((q / S) & 1))) break;
+        for (unsigned long long q = consumed; q < issued; q++) mbar_wait(&full[q % S], (unsigned)((q / S) & 1));
 }
 
 template <int BLOCK, int IPT>
