@@ -192,13 +192,14 @@ class ClockSampler:
 
 def cpu_baseline(ps, p, sample: int, threads: int, table=None, seconds: float = 10.0):
     """The reference algorithm on the host cores: the plain-C oracle (OpenMP
-    over i, sequential j, per-pair atomics, as StePS/src/forces.cc), timed on
-    the i range [N/2, N/2 + sample) against all N j. sample <= 0 sizes the
-    range from a short calibration run so that it takes about `seconds`."""
+    over i, sequential j, per-pair atomics, as StePS/src/forces.cc) built with
+    the reference's release flags (-O3 -ffast-math), timed on the i range
+    [N/2, N/2 + sample) against all N j. sample <= 0 sizes the range from a
+    short calibration run so that it takes about `seconds`."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
 
-    port = pyoracle.Port(threads=threads)
+    port = pyoracle.Port(threads=threads, release=True)
     tp = {0: 0, 1: 1, 2: 3 if p.s1r2_images else 2}[p.topology]
     tab, ng, nrho, nz = table if table else (None, 0, 0, 0)
     s = port.system(tp, ps.m, ps.eps, pyoracle.make_params(p.is_periodic, p.L, p.rsim), table=tab, ngrid=ng,
@@ -266,7 +267,8 @@ def run_reference(args, ws, rank):
             "warmup": args.warmup, "ms_per_step": float(sample * ps.n / v * 1e3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
             "config": {"workload": desc + ", CPU sample"},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": smp},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": smp,
+                             "build": "oracle port, -O3 -ffast-math (the reference's release flags)"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -466,6 +468,7 @@ def main():
         threads = os.cpu_count() or 1
         rate, dt, pairs, ni = cpu_baseline(ps, p, args.cpu_sample, threads, tab, seconds=args.cpu_seconds)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                                "build": "oracle port, -O3 -ffast-math (the reference's release flags)",
                                 "sample": f"{ni} i particles x all {ps.n} j ({dt:.1f} s of CPU work)"}
         print(json.dumps(line), flush=True)
     if dist is not None:

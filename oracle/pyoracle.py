@@ -19,6 +19,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "liboracle_steps.so")
+# -O3 -ffast-math build, the reference's release flags: CPU-baseline timing only
+PORT_RELEASE_SO = os.path.join(HERE, "_build", "liboracle_steps_release.so")
 REF_DIR = os.path.join(HERE, "_ref")
 
 _dp = C.POINTER(C.c_double)
@@ -58,10 +60,11 @@ def make_params(is_periodic=0, L=0.0, rsim=0.0, cosmology=0, comoving=0, mius=0.
 class Port:
     """The plain-C oracle. Arrays are float64 numpy; x is (N,3) C-contiguous."""
 
-    def __init__(self, threads: int | None = None):
-        if not os.path.exists(PORT_SO):
+    def __init__(self, threads: int | None = None, release: bool = False):
+        so = PORT_RELEASE_SO if release else PORT_SO
+        if not os.path.exists(so):
             build_port()
-        self.lib = C.CDLL(PORT_SO)
+        self.lib = C.CDLL(so)
         L = self.lib
         L.oracle_force_softening.restype = C.c_double
         L.oracle_force_softening.argtypes = [C.c_double, C.c_double]
