@@ -1,10 +1,11 @@
 """Device-resident KDK leapfrog (StePS/src/step.cc:100-312) against the
 reference's own step() (golden vectors: one force then 4 fixed-dt steps)."""
 import numpy as np
+import pyoracle as O
 import pytest
 
 import steps_gb300 as S
-from helpers import err_stats, golden, rel_err
+from helpers import err_stats, golden, port_params, rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -40,3 +41,48 @@ def test_kdk_needs_state(engine):
     with pytest.raises(S.StepsError) as e:
         engine.kdk(S.params(S.R3), S.FP64, 1, 1e-3)
     assert e.value.code == S.STEPS_E_STATE
+
+
+@pytest.mark.parametrize("topo", ["t3", "s1r2"])
+def test_kdk_periodic_wrap(engine, port, topo):
+    """KDK on the periodic topologies (the wrap of StePS/src/step.cc:151-180:
+    all axes on T^3, z on S1xR2), with velocities that carry many particles
+    across the boundary, against the oracle's KDK."""
+    if topo == "t3":
+        g = golden("t3_o2")
+        L, ng = float(g["L"]), int(g["ngrid"])
+        p = S.params(S.T3, is_periodic=2, L=L, rsim=L / 2, ewald_order=2)
+        engine.set_table_t3(g["table"], ng)
+        s = port.system(1, g["m"], g["eps"], port_params(O, is_periodic=2, L=L, rsim=L / 2), table=g["table"],
+                        ngrid=ng, order=2)
+        axes = 3
+    else:
+        g = golden("s1r2_images")
+        L = float(g["L"])
+        p = S.params(S.S1R2, is_periodic=2, L=L, rsim=float(g["rsim"]), s1r2_images=1)
+        s = port.system(3, g["m"], g["eps"], port_params(O, is_periodic=2, L=L, rsim=float(g["rsim"])))
+        axes = 1
+    x = g["x"].copy()
+    rng = np.random.default_rng(11)
+    h = 1e-3
+    v = np.zeros_like(x)
+    v[:, 3 - axes:] = rng.uniform(-1.0, 1.0, (x.shape[0], axes)) * (0.02 * L / h)  # up to 2 % of L per step
+    nsteps = 3
+    xo, vo, Fo, eo = port.kdk(s, nsteps, h, x, v, port.forces(s, x), rho_part=1.0)
+    lo, hi = (0.0, L)
+    assert ((xo[:, 3 - axes:] < lo + 0.06 * L) | (xo[:, 3 - axes:] > hi - 0.06 * L)).any()  # some wrapped
+    engine.set_particles(g["m"], g["eps"])
+    for precision, xtol, ftol in ((S.FP64, 1e-9, 1e-9), (S.MIXED, 1e-5, 1e-5)):
+        engine.upload_positions(x)
+        engine.upload_velocities(v)
+        e = engine.kdk(p, precision, nsteps, h, rho_part=1.0)
+        xg, vg, Fg = engine.state()
+        dx = np.abs(xg - xo)
+        dx = np.minimum(dx, L - dx) if topo == "t3" else np.concatenate(
+            [dx[:, :2], np.minimum(dx[:, 2:], L - dx[:, 2:])], axis=1)
+        assert dx.max() < xtol * L, (precision, dx.max())
+        assert ((xg[:, 3 - axes:] >= 0) & (xg[:, 3 - axes:] < L)).all()
+        if precision == S.FP64:
+            assert rel_err(Fg, Fo).max() < ftol
+        else:
+            assert err_stats(Fg, Fo)["p99"] < ftol
