@@ -106,7 +106,12 @@ __global__ void __launch_bounds__(BLOCK, KIND == K_R3 && IPT == 1 ? 1024 / BLOCK
 
             bool full;  // near-field tile pair: softening and every test per pair
             float off[NIMG];
-            unsigned strad = 0u;  // S1 images straddling the cut over this tile pair
+            unsigned long long strad = 0ull;  // S1 images straddling the cut over this tile pair
+            // K_S1_GEN with explicit images (any count): the images not entirely
+            // outside the cut form [mfirst, mlast]; bit m - mfirst of stradl marks
+            // those straddling it.
+            int mfirst = 0, mlast = -1;
+            unsigned long long stradl = 0ull;
             if (KIND == K_R3) {  // per warp: warps away from a near J keep the far loop
                 full = warp_full(dOx, dOy, dOz, wc, wh, mJ1, bmax, a.guard2);
             } else if (KIND == K_S1_IMG) {
@@ -120,14 +125,14 @@ __global__ void __launch_bounds__(BLOCK, KIND == K_R3 && IPT == 1 ? 1024 / BLOCK
                 bool near = false;
                 float g2min = 3.0e38f;
                 const float cin = a.cutL * (1.0f - 1e-6f), cout = a.cutL * (1.0f + 1e-6f);
-                strad = 0u;
+                strad = 0ull;
 #pragma unroll
                 for (int m = 0; m < NIMG; m++) {
                     const float sh = (float)(m - EMAX) * a.L;
                     const float l = lo + sh, h = hi + sh;
                     const bool in = fmaxf(fabsf(l), fabsf(h)) <= cin;
                     const bool out = l > cout || h < -cout;
-                    strad |= (in || out) ? 0u : 1u << m;
+                    strad |= (in || out) ? 0ull : 1ull << m;
                     off[m] = out ? 1e18f : sh;
                     const float gz = (l <= 0.0f && h >= 0.0f) ? 0.0f : fminf(fabsf(l), fabsf(h));
                     near |= !out && (g2xy + gz * gz <= bmax2);
@@ -144,7 +149,28 @@ __global__ void __launch_bounds__(BLOCK, KIND == K_R3 && IPT == 1 ? 1024 / BLOCK
                 full = fabsf(dOz) + mI1.z + mJ1.z > a.halfL - a.wrap_tol || g2 <= bmax2 ||
                        coarse_for_gap(dOx, dOy, dOz, mI1, mJ1, g2, a.guard2);
             } else {
-                full = true;
+                const float hz = mI1.z + mJ1.z;
+                const float lo = dOz - hz, hi = dOz + hz;
+                const float g2xy = gx * gx + gy * gy;
+                const float cin = a.cutL * (1.0f - 1e-6f), cout = a.cutL * (1.0f + 1e-6f);
+                bool near = false, many = false;
+                float g2min = 3.0e38f;
+                mfirst = a.emax + 1;
+                for (int m = -a.emax; m <= a.emax; m++) {
+                    const float sh = (float)m * a.L;
+                    const float l = lo + sh, h = hi + sh;
+                    if (l > cout || h < -cout) continue;  // entirely outside the cut
+                    if (mfirst > a.emax) mfirst = m;
+                    mlast = m;
+                    if (fmaxf(fabsf(l), fabsf(h)) > cin) {  // straddles the cut
+                        if (m - mfirst < 64) stradl |= 1ull << (m - mfirst);
+                        else many = true;
+                    }
+                    const float gz = (l <= 0.0f && h >= 0.0f) ? 0.0f : fminf(fabsf(l), fabsf(h));
+                    near |= g2xy + gz * gz <= bmax2;
+                    g2min = fminf(g2min, g2xy + gz * gz);
+                }
+                full = many || near || coarse_for_gap(dOx, dOy, dOz, mI1, mJ1, g2min, a.guard2);
             }
 
             // i in J's frame, rounded to FP32 for the far path.
@@ -161,8 +187,41 @@ __global__ void __launch_bounds__(BLOCK, KIND == K_R3 && IPT == 1 ? 1024 / BLOCK
             const uint32_t *sidb = sid[buf];
             const float4 *sresb = sres[buf];
 
-            if (!full) {
-                if (KIND == K_R3 || KIND == K_S1_GEN) {  // K_S1_GEN: nearest-image tile pairs only
+            if (!full && KIND == K_S1_GEN && !a.nearest) {
+                // explicit images, any count: a runtime loop over [mfirst, mlast]
+#pragma unroll 2
+                for (int jj = 0; jj < T; ++jj) {
+                    const float4 q = spb[jj];
+#pragma unroll
+                    for (int k = 0; k < IPT; k++) {
+                        const float dx = q.x - px[k], dy = q.y - py[k], dz = q.z - pz[k];
+                        const float rho2 = fmaf(dx, dx, dy * dy);
+                        float sw = 0.0f, swz = 0.0f, fm = (float)mfirst;
+                        for (int m = mfirst; m <= mlast; m++, fm += 1.0f) {
+                            const float sh = fm * a.L;
+                            const float dzm = dz + sh;
+                            const float ri = rsqrt_mufu(fmaf(dzm, dzm, rho2));
+                            float ri3 = ri * ri * ri;
+                            if (stradl >> (m - mfirst) & 1ull) {  // block-uniform
+                                bool in = fabsf(dzm) <= a.cutL;
+                                if (fabsf(fabsf(dzm) - a.cutL) < a.cut_tol) {
+                                    float phz, plz;
+                                    frame_split(zi[k], lz[k], dOz, eOz, phz, plz);
+                                    in = cut_in_exact(q.z, sresb[jj].z, phz, plz, sh, a.cutL);
+                                }
+                                ri3 = in ? ri3 : 0.0f;
+                            }
+                            sw += ri3;
+                            swz = fmaf(ri3, dzm, swz);
+                        }
+                        const float t = q.w * sw;
+                        fx[k] = fmaf(t, dx, fx[k]);
+                        fy[k] = fmaf(t, dy, fy[k]);
+                        fz[k] = fmaf(q.w, swz, fz[k]);
+                    }
+                }
+            } else if (!full) {
+                if (KIND == K_R3 || KIND == K_S1_GEN) {  // K_S1_GEN here: nearest-image tile pairs
 #pragma unroll 8
                     for (int jj = 0; jj < T; ++jj) {
                         const float4 q = spb[jj];
@@ -178,7 +237,7 @@ __global__ void __launch_bounds__(BLOCK, KIND == K_R3 && IPT == 1 ? 1024 / BLOCK
                         }
                     }
                 } else if (KIND == K_S1_IMG) {
-                    if (strad == 0u) {  // every image entirely in or out of the cut
+                    if (strad == 0ull) {  // every image entirely in or out of the cut
 #pragma unroll 2
                         for (int jj = 0; jj < T; ++jj) {
                             const float4 q = spb[jj];
@@ -214,7 +273,7 @@ __global__ void __launch_bounds__(BLOCK, KIND == K_R3 && IPT == 1 ? 1024 / BLOCK
                                     const float dzm = dz + off[m];
                                     const float ri = rsqrt_mufu(fmaf(dzm, dzm, rho2));
                                     float ri3 = ri * ri * ri;
-                                    if (strad & (1u << m)) {  // block-uniform
+                                    if (strad & (1ull << m)) {  // block-uniform
                                         bool in = fabsf(dzm) <= a.cutL;
                                         if (fabsf(fabsf(dzm) - a.cutL) < a.cut_tol) {
                                             float phz, plz;
@@ -362,6 +421,7 @@ KernelFn select_kernel(const KParams &kp, int threads, int ipt)
         case 3: return pick<K_S1_IMG, 3>(threads, ipt);
         case 4: return pick<K_S1_IMG, 4>(threads, ipt);
         case 5: return pick<K_S1_IMG, 5>(threads, ipt);
+        case 16: return pick<K_S1_IMG, 16>(threads, ipt);  // IS_PERIODIC = 15, the cylindrical example
         default: return pick<K_S1_GEN, 0>(threads, ipt);
         }
     }

@@ -70,6 +70,19 @@ def test_s1r2_images_mixed_large(engine):
     assert st["p99"] < MIXED_P99, st
 
 
+def test_s1r2_many_images_mixed(engine):
+    """IS_PERIODIC = 15 (33 images, the cylindrical example's setting): the
+    runtime image loop of the far path and its per-pair cut tests, full range
+    against an FP64 i subset."""
+    ps = W.s1r2_cylindrical(1 << 16, 100.0, 1000.0, seed=14)
+    engine.set_particles(ps.m, ps.eps)
+    p = S.params(S.S1R2, is_periodic=15, L=100.0, rsim=1000.0, s1r2_images=1)
+    Fm = engine.forces(ps.x, p, S.MIXED)
+    lo, hi = 30000, 30767
+    st = err_stats(Fm[lo:hi + 1], engine.forces(ps.x, p, S.FP64, lo, hi))
+    assert st["p99"] < MIXED_P99, st
+
+
 @pytest.mark.parametrize("order", [0, 2, 4])
 def test_s1r2_table_fp64(engine, order):
     g = golden(f"s1r2_table_o{order}")
