@@ -70,7 +70,7 @@ __global__ void __launch_bounds__(NA_THREADS)
     k_noalloc_fp64_r3(const double *__restrict__ x, const double *__restrict__ m, const double *__restrict__ eps,
                       int n, int id_min, int ni, int jchunk, double *__restrict__ part)
 {
-    __shared__ double4 sp[NA_THREADS];
+    __shared__ double4_16a sp[NA_THREADS];
     __shared__ double se[NA_THREADS];
     const int t = threadIdx.x;
     const int li = blockIdx.x * NA_THREADS + t;
@@ -85,12 +85,12 @@ __global__ void __launch_bounds__(NA_THREADS)
         __syncthreads();
         if (t < cnt) {
             const size_t j = (size_t)jb + t;
-            sp[t] = make_double4(x[3 * j], x[3 * j + 1], x[3 * j + 2], m[j]);
+            sp[t] = make_double4_16a(x[3 * j], x[3 * j + 1], x[3 * j + 2], m[j]);
             se[t] = eps[j];
         }
         __syncthreads();
         for (int jj = 0; jj < cnt; ++jj) {
-            const double4 q = sp[jj];
+            const double4_16a q = sp[jj];
             const double dx = q.x - xi, dy = q.y - yi, dz = q.z - zi;
             const double w = q.w * softening_fp64(dx * dx + dy * dy + dz * dz, ei + se[jj]);
             ax = fma(w, dx, ax);

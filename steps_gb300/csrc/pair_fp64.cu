@@ -145,15 +145,15 @@ __device__ __forceinline__ double nearest(double d, double L, double halfL)
 
 template <int MODE, int ORDER>
 __global__ void __launch_bounds__(FP64_THREADS)
-    k_pair_fp64(const double4 *__restrict__ pj, const double *__restrict__ ej, int n, int id_min, int ni, int jchunk,
+    k_pair_fp64(const double4_16a *__restrict__ pj, const double *__restrict__ ej, int n, int id_min, int ni, int jchunk,
                 KParams kp, Tables tb, double *__restrict__ part)
 {
-    __shared__ double4 sp[FP64_THREADS];
+    __shared__ double4_16a sp[FP64_THREADS];
     __shared__ double se[FP64_THREADS];
     int t = threadIdx.x;
     int li = blockIdx.x * FP64_THREADS + t;
     bool active = li < ni;
-    double4 pi = active ? pj[id_min + li] : make_double4(0, 0, 0, 0);
+    double4_16a pi = active ? pj[id_min + li] : make_double4_16a(0, 0, 0, 0);
     double ei = active ? ej[id_min + li] : 0.0;
     int j0 = blockIdx.y * jchunk;
     int j1 = min(n, j0 + jchunk);
@@ -169,7 +169,7 @@ __global__ void __launch_bounds__(FP64_THREADS)
         }
         __syncthreads();
         for (int jj = 0; jj < cnt; ++jj) {
-            double4 q = sp[jj];
+            double4_16a q = sp[jj];
             double b = ei + se[jj];
             double dx = q.x - pi.x, dy = q.y - pi.y, dz = q.z - pi.z;
             if (MODE == M_R3) {
@@ -238,10 +238,10 @@ __global__ void __launch_bounds__(FP64_THREADS)
     }
 }
 
-__global__ void k_pack64(const double *__restrict__ x, const double *__restrict__ m, int n, double4 *__restrict__ out)
+__global__ void k_pack64(const double *__restrict__ x, const double *__restrict__ m, int n, double4_16a *__restrict__ out)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) out[i] = make_double4(x[3 * (size_t)i], x[3 * (size_t)i + 1], x[3 * (size_t)i + 2], m[i]);
+    if (i < n) out[i] = make_double4_16a(x[3 * (size_t)i], x[3 * (size_t)i + 1], x[3 * (size_t)i + 2], m[i]);
 }
 
 }  // namespace
@@ -265,7 +265,7 @@ void launch_fp64(dim3 grid, int n, int id_min, int ni, int jchunk, const KParams
                  cudaStream_t st)
 {
     Ctx &c = ctx();
-    k_pair_fp64<MODE, ORDER><<<grid, FP64_THREADS, 0, st>>>(c.pack64.as<double4>(), c.eps64.as<double>(), n, id_min, ni,
+    k_pair_fp64<MODE, ORDER><<<grid, FP64_THREADS, 0, st>>>(c.pack64.as<double4_16a>(), c.eps64.as<double>(), n, id_min, ni,
                                                             jchunk, kp, tb, part);
     note_launch("k_pair_fp64");
 }
@@ -296,9 +296,9 @@ void forces_fp64(const KParams &kp, const Tables &tb, const double *x, int n, in
 {
     Ctx &c = ctx();
     cudaStream_t st = c.stream;
-    c.pack64.ensure<double4>(n);
+    c.pack64.ensure<double4_16a>(n);
     STEPS_CUDA(cudaEventRecord(c.phase[0], st));
-    k_pack64<<<div_up(n, 256), 256, 0, st>>>(x, c.m64.as<double>(), n, c.pack64.as<double4>());
+    k_pack64<<<div_up(n, 256), 256, 0, st>>>(x, c.m64.as<double>(), n, c.pack64.as<double4_16a>());
     note_launch("k_pack64");
     STEPS_CUDA(cudaEventRecord(c.phase[1], st));
 

@@ -70,7 +70,7 @@ __device__ __forceinline__ void stencil(const float *wx, const float *wy, const 
                                         float &Dy, float &Dz)
 {
     constexpr int NT = ORDER;
-    if (ORDER == 4) {
+    if constexpr (ORDER == 4) {
 #pragma unroll
         for (int aa = 0; aa < NT; aa++) {
             float rx = 0.0f, ry = 0.0f, rz = 0.0f;
@@ -92,22 +92,22 @@ __device__ __forceinline__ void stencil(const float *wx, const float *wy, const 
             Dy = fmaf(wx[aa], ry, Dy);
             Dz = fmaf(wx[aa], rz, Dz);
         }
-        return;
-    }
+    } else {
 #pragma unroll
-    for (int aa = 0; aa < NT; aa++)
+        for (int aa = 0; aa < NT; aa++)
 #pragma unroll
-        for (int bb = 0; bb < NT; bb++) {
-            const float wxy = wx[aa] * wy[bb];
+            for (int bb = 0; bb < NT; bb++) {
+                const float wxy = wx[aa] * wy[bb];
 #pragma unroll
-            for (int cc = 0; cc < NT; cc++) {
-                const float4 v = fetch(aa, bb, cc);
-                const float ww = wxy * wz[cc];
-                Dx = fmaf(ww, v.x, Dx);
-                Dy = fmaf(ww, v.y, Dy);
-                Dz = fmaf(ww, v.z, Dz);
+                for (int cc = 0; cc < NT; cc++) {
+                    const float4 v = fetch(aa, bb, cc);
+                    const float ww = wxy * wz[cc];
+                    Dx = fmaf(ww, v.x, Dx);
+                    Dy = fmaf(ww, v.y, Dy);
+                    Dz = fmaf(ww, v.z, Dz);
+                }
             }
-        }
+    }
 }
 
 // ORDER 0: IS_PERIODIC == 1, nearest image only (no table).
