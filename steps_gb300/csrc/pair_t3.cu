@@ -727,19 +727,20 @@ __global__ void k_table_records(const double *__restrict__ t, int ng, int halo, 
     for (int comp = 0; comp < 3; comp++) out[3 * c + comp] = make_float4(v[comp][0], v[comp][1], v[comp][2], v[comp][3]);
 }
 
-// Halo of the FP32 table copy: tile pairs whose stencils stay within it need
-// no per-pair index wrap.
-constexpr int T3_HALO = 16;
+// Halo of the FP32 table copies: tile pairs whose stencils stay within it
+// need no per-pair wrap. It grows with the grid (cells shrink as L / ng, tile
+// extents do not): 16 cells at ng = 63, ng / 8 above 128.
+inline int t3_halo(int ng) { return ng / 8 > 16 ? ng / 8 : 16; }
 
 // FP32 float4 haloed copy of the FP64 table, rebuilt whenever the table changes.
 const float4 *t3_table_f32(const Tables &tb, cudaStream_t st)
 {
     Ctx &c = ctx();
-    const size_t ext = (size_t)tb.t3_ng + 2 * T3_HALO;
+    const size_t ext = (size_t)tb.t3_ng + 2 * t3_halo(tb.t3_ng);
     const size_t ncell = ext * ext * ext;
     if (c.t3f_version != c.t3_version || !c.t3f.p) {
         float4 *o = c.t3f.ensure<float4>(ncell);
-        k_table_f32<<<(unsigned)((ncell + 255) / 256), 256, 0, st>>>(tb.t3, tb.t3_ng, T3_HALO, o);
+        k_table_f32<<<(unsigned)((ncell + 255) / 256), 256, 0, st>>>(tb.t3, tb.t3_ng, t3_halo(tb.t3_ng), o);
         note_launch("k_table_f32");
         c.t3f_version = c.t3_version;
     }
@@ -751,11 +752,12 @@ const float4 *t3_table_f32(const Tables &tb, cudaStream_t st)
 const float4 *t3_table_records(const Tables &tb, int order, cudaStream_t st)
 {
     Ctx &c = ctx();
-    const size_t ext = (size_t)tb.t3_ng + 2 * T3_HALO;
+    const size_t ext = (size_t)tb.t3_ng + 2 * t3_halo(tb.t3_ng);
     const size_t ncell = ext * ext * ext;
     if (c.t3r_version != c.t3_version || c.t3r_order != order || !c.t3r.p) {
         float4 *o = c.t3r.ensure<float4>(3 * ncell);
-        k_table_records<<<(unsigned)((ncell + 255) / 256), 256, 0, st>>>(tb.t3, tb.t3_ng, T3_HALO, order, o);
+        k_table_records<<<(unsigned)((ncell + 255) / 256), 256, 0, st>>>(tb.t3, tb.t3_ng, t3_halo(tb.t3_ng), order,
+                                                                          o);
         note_launch("k_table_records");
         c.t3r_version = c.t3_version;
         c.t3r_order = order;
@@ -770,8 +772,8 @@ void t3_args(MixedArgs &a, const KParams &kp, const Tables &tb, cudaStream_t st)
     a.ih = 0.0f;
     a.u0 = 0.0f;
     a.wcap = ctx().shape.t3_cells;
-    a.halo = T3_HALO;
-    a.ext = tb.t3_ng + 2 * T3_HALO;
+    a.halo = t3_halo(tb.t3_ng);
+    a.ext = tb.t3_ng + 2 * a.halo;
     a.t3r = nullptr;
     if (kp.is_periodic >= 2) {
         a.t3f = t3_table_f32(tb, st);
