@@ -16,7 +16,11 @@ reference). Other workloads (--workload):
 
 --impl reference times the reference algorithm's CPU implementation (the
 plain-C oracle restating StePS/src/forces.cc, OpenMP over all host cores) on
-a bounded i-subset sample of the same workload.
+a bounded i-subset sample of the same workload. With --ref-device gpu it
+times instead the reference's own CUDA kernels (StePS/src/forces_cuda.cu,
+compiled unmodified into oracle/_ref/*.cubin) with the reference's launch
+shape, in its FP32 and FP64 builds, on one full wave of i particles against a
+j subset sized to about --ref-seconds per launch.
 
 With --gpus N > 1 (torchrun) every rank evaluates its own independent
 realisation (seed + rank): weak scaling, no collective on the data path.
@@ -56,6 +60,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--ref-device", default="cpu", choices=["cpu", "gpu"],
+                    help="--impl reference: the reference's CPU path (default) or its own CUDA kernels")
+    ap.add_argument("--ref-seconds", type=float, default=1.0, help="--ref-device gpu: target time of one launch")
     ap.add_argument("--workload", default="cfg1", choices=["cfg0", "cfg1", "cfg2", "cfg3", "cfg4"])
     ap.add_argument("--batch-scale", type=float, default=1.0, help="cfg4: scale every N_k (small test runs)")
     ap.add_argument("--order", type=int, default=2,
@@ -89,6 +96,14 @@ def workload(args, rank=0):
         ps = W.r3_compactified(n, rmax, seed=(0 if w == "cfg0" else 1) + rank, displace=(w == "cfg1"))
         desc = f"R3 compactified N={n} R_max={rmax:g} Mpc" + (", clustered (sigma=0.5 spacing)" if w == "cfg1" else "")
         return ps, S.params(S.R3), 20, desc, None
+    if w == "cfg4":
+        # The reference arms time the ensemble's force path on its largest
+        # realisation: the per-pair cost does not depend on N.
+        sets = W.r3_ensemble(64, scale=args.batch_scale)
+        k = int(np.argmax([s.n for s in sets]))
+        desc = (f"batched ensemble of {len(sets)} R3 realisations (N_k log-uniform [8192, 262144]), "
+                f"timed on its largest, realisation {k} (N={sets[k].n})")
+        return sets[k], S.params(S.R3), 20, desc, None
     if w == "cfg2":
         n = args.n or (1 << 21)
         ps = W.s1r2_cylindrical(n, 200.0, 600.0, seed=2 + rank)
@@ -273,6 +288,79 @@ def run_reference(args, ws, rank):
     print(json.dumps(line), flush=True)
 
 
+def run_reference_gpu(args, ws, rank):
+    """The reference's CUDA kernels (oracle/refgpu.py) on this workload: FP32
+    build (USE_SINGLE_PRECISION) and FP64 build, kernel time only, with the
+    FP32 build's error against the FP64 build on the same sample."""
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import refgpu
+
+    ps, p, flops, desc, table = workload(args)
+    base = {0: "r3", 1: "t3", 2: "s1nl"}[p.topology]
+    if p.topology == 1:
+        flops = 33 + 494  # tricubic
+    why = None
+    if table and table["kind"] == "s1":
+        why = "the reference's S1xR2 table kernel is not wired into oracle/refgpu.py"
+    elif not (refgpu.available(base) and refgpu.available(base + "sp")):
+        why = "oracle/_ref/forces_cuda_*.cubin not built (needs the reference tree at build time)"
+    if why:
+        print(json.dumps({"impl": "reference", "device": "gpu", "unavailable": why}), flush=True)
+        return
+    kw = {}
+    if p.topology == 1:
+        kw = {"is_periodic": p.is_periodic, "L": p.L}
+    elif p.topology == 2:
+        kw = {"is_periodic": p.is_periodic, "L": p.L, "rsim": p.rsim}
+    tab = host_table(table)
+    res = {}
+    for v in (base + "sp", base):
+        k = refgpu.RefKernel(v)
+        k.set_particles(ps.x, ps.m, ps.eps)
+        if tab is not None:
+            k.set_table_t3(tab[0], tab[1])
+        ni = min(ps.n, k.wave())
+        nj = min(ps.n, 1024)
+        ms, _ = k.time(0, ni - 1, nj, steps=1, warmup=1, **kw)  # calibration
+        nj = int(min(ps.n, max(nj, nj * args.ref_seconds * 1e3 / max(ms, 1e-3))))
+        ms, F = k.time(0, ni - 1, nj, steps=args.steps, warmup=args.warmup, **kw)
+        res[v] = {"pairs_per_s": ni * nj / (ms * 1e-3), "kernel_ms": ms, "i": ni, "j": nj, "F": F,
+                  "registers": k.registers, "blocks_per_sm": k.blocks_per_sm}
+    a, b = res[base + "sp"], res[base]
+    Fb = b["F"]
+    if a["j"] == b["j"]:
+        Fa = a["F"]
+    else:  # the FP32 build on the FP64 build's sample for the error figures
+        k = refgpu.RefKernel(base + "sp")
+        k.set_particles(ps.x, ps.m, ps.eps)
+        if tab is not None:
+            k.set_table_t3(tab[0], tab[1])
+        Fa = k.forces(0, b["i"] - 1, b["j"], **kw)
+    rel = np.linalg.norm(Fa - Fb, axis=1) / np.maximum(np.linalg.norm(Fb, axis=1), 1e-300)
+    v = a["pairs_per_s"]
+    interp = ", tricubic (the reference GPU kernel's only T^3 interpolation)" if p.topology == 1 else ""
+    line = {"impl": "reference", "device": "gpu", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": a["kernel_ms"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (the reference's USE_SINGLE_PRECISION build)",
+            "data": "synthetic (seeded)",
+            "config": {"workload": desc + interp,
+                       "sample": f"i = one full wave of resident blocks ({a['i']}), j = the first {a['j']} "
+                                 f"particles (FP64 build: {b['j']}); pair cost does not depend on N",
+                       "launch": "32 x SMs blocks of 256 threads, grid-stride i loop (StePS/src/forces_cuda.cu:1053)",
+                       "source": "StePS/src/forces_cuda.cu compiled unmodified for sm_103a (nvcc -O3)"},
+            "roofline": {"bound": "fp32", "achieved": v * flops / 1e12, "unit": "TFLOP/s",
+                         "flops_per_pair": flops},
+            "fp32_build": {k_: a[k_] for k_ in ("pairs_per_s", "kernel_ms", "i", "j", "registers", "blocks_per_sm")},
+            "fp64_build": {k_: b[k_] for k_ in ("pairs_per_s", "kernel_ms", "i", "j", "registers", "blocks_per_sm")},
+            "accuracy_fp32_vs_fp64": {"p50": float(np.percentile(rel, 50)), "p99": float(np.percentile(rel, 99)),
+                                      "max": float(rel.max()), "sample": f"{b['i']} i x {b['j']} j"},
+            "e2e": None, "e2e_note": "kernel time only; the reference wrapper's per-call allocations and copies "
+                                     "(forces_cuda.cu:976-1105) are not timed"}
+    print(json.dumps(line), flush=True)
+
+
 def run_ours(args, ws, rank, local, dist):
     import steps_gb300 as S
 
@@ -453,7 +541,10 @@ def main():
     args = parse()
     ws, rank, local = dist_env()
     if args.impl == "reference":
-        run_reference(args, ws, rank)
+        if args.ref_device == "gpu":
+            run_reference_gpu(args, ws, rank)
+        else:
+            run_reference(args, ws, rank)
         return
     dist = dist_init(ws)
     if args.workload == "cfg4":

@@ -1,0 +1,141 @@
+"""The reference's own CUDA force kernels (StePS/src/forces_cuda.cu, compiled
+unmodified into oracle/_ref/forces_cuda_*.cubin and launched with the
+reference's grid by oracle/refgpu.py) on the GPU:
+
+* FP64 builds against the golden vectors of the reference's CPU build and
+  against this library's FP64 kernels on the same inputs: the reference's
+  GPU path, its CPU path, the oracle and the new kernels agree to 1e-12.
+* FP32 builds (USE_SINGLE_PRECISION, REAL = float): the error floor of the
+  reference's own single-precision GPU path against its FP64 result; the
+  mixed kernels must be at least as accurate in p99 and max.
+
+The cubins are built where the reference tree is; without them these tests
+skip."""
+import numpy as np
+import pytest
+
+import steps_gb300 as S
+from helpers import err_stats, golden, rel_err
+from steps_gb300 import workloads as W
+
+refgpu = pytest.importorskip("refgpu")
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+
+
+def kernel(variant):
+    if not refgpu.available(variant):
+        pytest.skip(f"reference kernel {variant} not built (oracle/_ref/forces_cuda_{variant}.cubin)")
+    return refgpu.RefKernel(variant)
+
+
+def check_floor(ours, theirs, what):
+    print(what, "mixed", ours, "reference FP32 GPU build", theirs)
+    assert ours["p99"] <= theirs["p99"] and ours["max"] <= theirs["max"], (what, ours, theirs)
+
+
+def test_r3_fp64_against_golden():
+    g = golden("r3_n2048")
+    k = kernel("r3")
+    k.set_particles(g["x"], g["m"], g["eps"])
+    assert rel_err(k.forces(), g["F"]).max() < FP64_TOL
+    lo, hi = (int(v) for v in g["sub"])
+    assert rel_err(k.forces(lo, hi), g["F_sub"]).max() < FP64_TOL
+    assert rel_err(k.forces(cosmology=1, comoving=1, mius=float(g["mius"])), g["F_comoving"]).max() < FP64_TOL
+    de = float(g["h0"]) ** 2 * float(g["oml"])
+    assert rel_err(k.forces(cosmology=1, comoving=0, de=de), g["F_de"]).max() < FP64_TOL
+
+
+def test_t3_fp64_against_golden():
+    """The reference GPU kernel always interpolates tricubically
+    (StePS/src/forces_cuda.cu:113-167): it matches the CPU build at
+    EWALD_INTERPOLATION_ORDER = 4, and with IS_PERIODIC = 1 the nearest-image
+    sum."""
+    g = golden("t3_o4")
+    L = float(g["L"])
+    k = kernel("t3")
+    k.set_particles(g["x"], g["m"], g["eps"])
+    k.set_table_t3(g["table"], int(g["ngrid"]))
+    assert rel_err(k.forces(is_periodic=2, L=L), g["F"]).max() < FP64_TOL
+    assert rel_err(k.forces(is_periodic=1, L=L), g["F_nearest"]).max() < FP64_TOL
+
+
+def test_s1r2_images_fp64_against_golden():
+    g = golden("s1r2_images")
+    L, rsim = float(g["L"]), float(g["rsim"])
+    k = kernel("s1nl")
+    k.set_particles(g["x"], g["m"], g["eps"])
+    assert rel_err(k.forces(is_periodic=2, L=L, rsim=rsim), g["F_is2"]).max() < FP64_TOL
+    assert rel_err(k.forces(is_periodic=1, L=L, rsim=rsim), g["F_is1"]).max() < FP64_TOL
+    assert rel_err(k.forces(0, 255, is_periodic=4, L=L, rsim=rsim), g["F_is4_head"]).max() < FP64_TOL
+
+
+def test_r3_fp64_against_ours_n16384(engine):
+    """The headline geometry at N = 16,384: the reference's FP64 GPU kernel
+    and this library's FP64 kernel on every particle."""
+    ps = W.r3_compactified(16384, 1000.0, seed=41, displace=True)
+    k = kernel("r3")
+    k.set_particles(ps.x, ps.m, ps.eps)
+    engine.set_particles(ps.m, ps.eps)
+    F = engine.forces(ps.x, S.params(S.R3), S.FP64)
+    assert rel_err(F, k.forces()).max() < FP64_TOL
+
+
+def test_t3_fp64_against_ours(engine):
+    """T^3 with the reference's Ng = 63 table geometry (built by this library,
+    which matches the reference's builder to 1e-13) at N = 4096, clumpy."""
+    ps = W.t3_clumpy(4096, 100.0, seed=43)
+    engine.set_particles(ps.m, ps.eps)
+    engine.build_table_t3(63, 100.0, 2.0 / 100.0, 2.0, 5.0 * 2.0 * np.pi / 100.0, 3.0, 6.0)
+    k = kernel("t3")
+    k.set_particles(ps.x, ps.m, ps.eps)
+    k.set_table_t3(engine.get_table_t3(63), 63)
+    F = engine.forces(ps.x, S.params(S.T3, is_periodic=2, L=100.0, rsim=50.0, ewald_order=4), S.FP64)
+    assert rel_err(F, k.forces(is_periodic=2, L=100.0)).max() < FP64_TOL
+
+
+def test_r3_fp32_floor(engine):
+    ps = W.r3_compactified(32768, 480.0, seed=0)
+    lo, hi = 16384, 16384 + 2047
+    k64, k32 = kernel("r3"), kernel("r3sp")
+    k64.set_particles(ps.x, ps.m, ps.eps)
+    k32.set_particles(ps.x, ps.m, ps.eps)
+    F64 = k64.forces(lo, hi)
+    engine.set_particles(ps.m, ps.eps)
+    F = engine.forces(ps.x, S.params(S.R3), S.MIXED)[lo:hi + 1]
+    check_floor(err_stats(F, F64), err_stats(k32.forces(lo, hi), F64), "R3 N=32768")
+
+
+def test_t3_fp32_floor(engine):
+    g = golden("t3_o4")
+    L = float(g["L"])
+    k = kernel("t3sp")
+    k.set_particles(g["x"], g["m"], g["eps"])
+    k.set_table_t3(g["table"], int(g["ngrid"]))
+    engine.set_particles(g["m"], g["eps"])
+    engine.set_table_t3(g["table"], int(g["ngrid"]))
+    F = engine.forces(g["x"], S.params(S.T3, is_periodic=2, L=L, rsim=L / 2, ewald_order=4), S.MIXED)
+    check_floor(err_stats(F, g["F"]), err_stats(k.forces(is_periodic=2, L=L), g["F"]), "T3 tricubic")
+
+
+def test_s1r2_fp32_floor(engine):
+    g = golden("s1r2_images")
+    L, rsim = float(g["L"]), float(g["rsim"])
+    k = kernel("s1nlsp")
+    k.set_particles(g["x"], g["m"], g["eps"])
+    engine.set_particles(g["m"], g["eps"])
+    p = S.params(S.S1R2, is_periodic=2, L=L, rsim=rsim, s1r2_images=1)
+    F = engine.forces(g["x"], p, S.MIXED)
+    check_floor(err_stats(F, g["F_is2"]), err_stats(k.forces(is_periodic=2, L=L, rsim=rsim), g["F_is2"]),
+                "S1xR2 images")
+
+
+def test_bad_ranges_are_refused():
+    k = kernel("r3")
+    k.set_particles(np.zeros((4, 3)), np.ones(4), np.ones(4))
+    with pytest.raises(ValueError):
+        k.forces(0, 4)
+    with pytest.raises(ValueError):
+        k.forces(0, 3, nj=5)
