@@ -288,6 +288,16 @@ def run_reference(args, ws, rank):
     print(json.dumps(line), flush=True)
 
 
+def set_ref_table(k, tab):
+    """Hands host_table()'s (table, ngrid, nrho, nz) to a reference kernel."""
+    if tab is None:
+        return
+    if tab[1]:
+        k.set_table_t3(tab[0], tab[1])
+    else:
+        k.set_table_s1r2(tab[0], tab[2], tab[3])
+
+
 def run_reference_gpu(args, ws, rank):
     """The reference's CUDA kernels (oracle/refgpu.py) on this workload: FP32
     build (USE_SINGLE_PRECISION) and FP64 build, kernel time only, with the
@@ -301,10 +311,10 @@ def run_reference_gpu(args, ws, rank):
     base = {0: "r3", 1: "t3", 2: "s1nl"}[p.topology]
     if p.topology == 1:
         flops = 33 + 494  # tricubic
-    why = None
     if table and table["kind"] == "s1":
-        why = "the reference's S1xR2 table kernel is not wired into oracle/refgpu.py"
-    elif not (refgpu.available(base) and refgpu.available(base + "sp")):
+        base = f"s1o{p.ewald_order}"
+    why = None
+    if not (refgpu.available(base) and refgpu.available(base + "sp")):
         why = "oracle/_ref/forces_cuda_*.cubin not built (needs the reference tree at build time)"
     if why:
         print(json.dumps({"impl": "reference", "device": "gpu", "unavailable": why}), flush=True)
@@ -319,8 +329,7 @@ def run_reference_gpu(args, ws, rank):
     for v in (base + "sp", base):
         k = refgpu.RefKernel(v)
         k.set_particles(ps.x, ps.m, ps.eps)
-        if tab is not None:
-            k.set_table_t3(tab[0], tab[1])
+        set_ref_table(k, tab)
         ni = min(ps.n, k.wave())
         nj = min(ps.n, 1024)
         ms, _ = k.time(0, ni - 1, nj, steps=1, warmup=1, **kw)  # calibration
@@ -335,8 +344,7 @@ def run_reference_gpu(args, ws, rank):
     else:  # the FP32 build on the FP64 build's sample for the error figures
         k = refgpu.RefKernel(base + "sp")
         k.set_particles(ps.x, ps.m, ps.eps)
-        if tab is not None:
-            k.set_table_t3(tab[0], tab[1])
+        set_ref_table(k, tab)
         Fa = k.forces(0, b["i"] - 1, b["j"], **kw)
     rel = np.linalg.norm(Fa - Fb, axis=1) / np.maximum(np.linalg.norm(Fb, axis=1), 1e-300)
     v = a["pairs_per_s"]

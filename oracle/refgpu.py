@@ -17,6 +17,10 @@ Kernels, with the signatures StePS/src/forces_cuda.cu declares:
                           (forces_cuda.cu:113-167) whatever the CPU order
   ForceKernel_periodic_z  forces_cuda.cu:652  S1xR2 z-image sum
                           (PERIODIC_Z_NOLOOKUP)
+  ForceKernel_periodic_z  forces_cuda.cu:764  S1xR2 nearest z image and the
+                          (rho, z) correction table, NGP / CIC / TSC by
+                          EWALD_INTERPOLATION_ORDER 0 / 2 / 4
+                          (forces_cuda.cu:180-442), rho_max = 2.25 Rsim
 Each reads x, M and SOFT_LENGTH as separate REAL arrays, computes the i in
 [ID_min, ID_max] against the j in [0, N) and ADDS into F[3 (i - ID_min) + k]
 (the reference's host wrapper uploads a zeroed F first, forces_cuda.cu:1045).
@@ -37,7 +41,11 @@ BLOCKS_PER_SM = 32  # the grid is 32 x SMs blocks, forces_cuda.cu:1053
 
 # variant -> (topology, REAL type code of the Itanium C++ ABI)
 VARIANTS = {"r3": ("R3", "d"), "r3sp": ("R3", "f"), "t3": ("T3", "d"), "t3sp": ("T3", "f"),
-            "s1nl": ("S1", "d"), "s1nlsp": ("S1", "f")}
+            "s1nl": ("S1", "d"), "s1nlsp": ("S1", "f"),
+            "s1o0": ("S1T", "d"), "s1o2": ("S1T", "d"), "s1o4": ("S1T", "d"),
+            "s1o0sp": ("S1T", "f"), "s1o2sp": ("S1T", "f"), "s1o4sp": ("S1T", "f")}
+# EWALD_LOOKUP_TABLE_RADIAL_EXTENT_FACTOR (StePS/src/global_variables.h:39)
+S1_RHO_EXTENT = 2.25
 
 
 def cubin_path(variant: str) -> str:
@@ -50,11 +58,14 @@ def available(variant: str = "r3") -> bool:
 
 def kernel_name(topology: str, t: str) -> str:
     """Mangled (Itanium C++ ABI) name of the reference kernel with REAL = t:
-    the parameter lists of forces_cuda.cu:522, :567 and :652."""
+    the parameter lists of forces_cuda.cu:522, :567, :652 and :764 (size_t
+    is unsigned long, m)."""
     if topology == "R3":
         return f"_Z11ForceKerneliiPK{t}S0_S0_P{t}S0_S0_{t}{t}iiii"
     if topology == "T3":
         return f"_Z20ForceKernel_periodiciiPK{t}S0_S0_P{t}iS0_S0_{t}S0_iii"
+    if topology == "S1T":
+        return f"_Z22ForceKernel_periodic_ziiPK{t}S0_S0_P{t}iS0_S0_{t}{t}{t}S0_iS0_mm{t}iiii"
     return f"_Z22ForceKernel_periodic_ziiPK{t}S0_S0_P{t}iS0_S0_{t}{t}{t}S0_{t}{t}iiii"
 
 
@@ -150,6 +161,15 @@ class RefKernel:
         self._table = self.torch.as_tensor(table, device=self.device).to(self.dtype).contiguous()
         self._ngrid = ngrid
 
+    def set_table_s1r2(self, table, nrho: int, nz: int):
+        """The (rho, z) table as the reference stores it, nrho x nz x 2, over
+        rho in [0, 2.25 Rsim] (the Rsim passed at launch)."""
+        table = np.asarray(table, dtype=np.float64).ravel()
+        if nrho < 2 or nz < 1 or table.size != nrho * nz * 2:
+            raise ValueError("S1xR2 table must hold nrho x nz x 2 values, nrho >= 2")
+        self._table = self.torch.as_tensor(table, device=self.device).to(self.dtype).contiguous()
+        self._nrho, self._nz = nrho, nz
+
     def _args(self, F, id_min, id_max, nj, is_periodic, L, rsim, mius, de, cosmology, comoving):
         R, I, P = self.real, C.c_int, C.c_void_p
         head = [I(self.stride), I(nj), P(self.xx.data_ptr()), P(self.xy.data_ptr()), P(self.xz.data_ptr()),
@@ -162,6 +182,15 @@ class RefKernel:
                 raise ValueError("the T^3 kernel with IS_PERIODIC >= 2 needs an Ewald table")
             vals = head + [I(is_periodic), P(self.m.data_ptr()), P(self.eps.data_ptr()), R(L),
                            P(self._table.data_ptr()), I(self._ngrid), I(id_min), I(id_max)]
+        elif self.topology == "S1T":
+            if is_periodic >= 2 and getattr(self, "_nrho", 0) <= 0:
+                raise ValueError("the S1xR2 table kernel with IS_PERIODIC >= 2 needs a (rho, z) table")
+            if cosmology:
+                raise ValueError("the cylindrical background table is not wired for the reference S1xR2 kernel")
+            vals = head + [I(is_periodic), P(self.m.data_ptr()), P(self.eps.data_ptr()), R(L), R(rsim), R(mius),
+                           P(self._table.data_ptr()), I(1), P(self._table.data_ptr()),
+                           C.c_size_t(getattr(self, "_nrho", 0)), C.c_size_t(getattr(self, "_nz", 0)), R(de),
+                           I(cosmology), I(comoving), I(id_min), I(id_max)]
         else:
             if cosmology:
                 raise ValueError("the cylindrical background table is not wired for the reference S1xR2 kernel")

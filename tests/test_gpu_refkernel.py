@@ -72,6 +72,35 @@ def test_s1r2_images_fp64_against_golden():
     assert rel_err(k.forces(0, 255, is_periodic=4, L=L, rsim=rsim), g["F_is4_head"]).max() < FP64_TOL
 
 
+@pytest.mark.parametrize("order", [0, 2, 4])
+def test_s1r2_table_fp64_against_golden(order):
+    """The reference's (rho, z) table kernel (forces_cuda.cu:764) built at
+    EWALD_INTERPOLATION_ORDER 0 / 2 / 4 against its CPU build."""
+    g = golden(f"s1r2_table_o{order}")
+    nrho, nz = (int(v) for v in g["shape"])
+    L, rsim = float(g["L"]), float(g["rsim"])
+    k = kernel(f"s1o{order}")
+    k.set_particles(g["x"], g["m"], g["eps"])
+    k.set_table_s1r2(g["table"], nrho, nz)
+    assert rel_err(k.forces(is_periodic=2, L=L, rsim=rsim), g["F"]).max() < FP64_TOL
+
+
+@pytest.mark.parametrize("order", [0, 2, 4])
+def test_s1r2_table_fp32_floor(engine, order):
+    g = golden(f"s1r2_table_o{order}")
+    nrho, nz = (int(v) for v in g["shape"])
+    L, rsim = float(g["L"]), float(g["rsim"])
+    k = kernel(f"s1o{order}sp")
+    k.set_particles(g["x"], g["m"], g["eps"])
+    k.set_table_s1r2(g["table"], nrho, nz)
+    engine.set_particles(g["m"], g["eps"])
+    engine.set_table_s1r2(g["table"], nrho, nz)
+    p = S.params(S.S1R2, is_periodic=2, L=L, rsim=rsim, s1r2_images=0, ewald_order=order)
+    F = engine.forces(g["x"], p, S.MIXED)
+    check_floor(err_stats(F, g["F"]), err_stats(k.forces(is_periodic=2, L=L, rsim=rsim), g["F"]),
+                f"S1xR2 table order {order}")
+
+
 def test_r3_fp64_against_ours_n16384(engine):
     """The headline geometry at N = 16,384: the reference's FP64 GPU kernel
     and this library's FP64 kernel on every particle."""
