@@ -50,7 +50,7 @@ struct MixedArgs {
     const float4 *s1rec;  // z-triplet records of s1tab (CIC, TSC)
     int nrho, nz;
     float irho, iz, rho_max;  // 1 / drho, nz / L_z
-    double s1_rho_max, s1_idrho, s1_idz, s1_L;  // the same in FP64 (exact NGP decisions)
+    double s1_drho, s1_dzc, s1_L;  // rho and z cell sizes and L in FP64 (exact NGP face decisions)
 };
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem)

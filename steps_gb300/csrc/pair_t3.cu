@@ -471,18 +471,28 @@ __device__ __forceinline__ double exact_sep(float q, float ph, float ql, float p
     return (double)s + ((double)e + ((double)ql - (double)pl));
 }
 
-// NGP cell of the separation (dx, dy, dz), dz already the nearest image, in
-// FP64 as StePS/src/ewald_space.cc:803-840 computes it (up to 1 ulp in the
-// scaled indices).
-__device__ __forceinline__ void ngp_index_fp64(double dx, double dy, double dz, const MixedArgs &a, int &ir, int &iz)
+// NGP cell within FP32 rounding of a face, decided on the FP64 separation
+// without a square root. The reference's index is floor(rho / drho + 1/2)
+// (StePS/src/ewald_space.cc:803-840); with K the integer nearest to the FP32
+// estimate of rho / drho + 1/2, it is K when rho >= (K - 1/2) drho, else K - 1,
+// and rho >= f >= 0 is rho^2 >= f^2. Exact up to the FP64 rounding of rho^2
+// and of the face: a pair within an ulp or so of a face may differ from the
+// reference's own FP64 rounding.
+__device__ __forceinline__ int ngp_rho_index(double dx, double dy, float ur_half, const MixedArgs &a)
 {
-    double rho = sqrt(dx * dx + dy * dy);
-    rho = rho < 0.0 ? 0.0 : (rho > a.s1_rho_max ? a.s1_rho_max : rho);
-    // products with the FP64 reciprocals: within 1 ulp of the reference's quotients
-    const double ur = rho * a.s1_idrho;
-    const double uz = (dz + 0.5 * a.s1_L) * a.s1_idz - 0.5;
-    ir = min(max((int)floor(ur + 0.5), 0), a.nrho - 1);
-    iz = wrap_near((float)floor(uz + 0.5), a.nz);
+    const float K = rintf(ur_half);
+    if (!(K > 0.0f)) return 0;
+    const double face = ((double)K - 0.5) * a.s1_drho;
+    const int ir = fma(dx, dx, dy * dy) >= face * face ? (int)K : (int)K - 1;
+    return min(max(ir, 0), a.nrho - 1);
+}
+
+// The same along z: floor((dz + L/2) / dz_cell) is K when dz + L/2 >= K dz_cell.
+__device__ __forceinline__ int ngp_z_index(double dz, float uz_half, const MixedArgs &a)
+{
+    const float K = rintf(uz_half);
+    const int iz = dz + 0.5 * a.s1_L >= (double)K * a.s1_dzc ? (int)K : (int)K - 1;
+    return wrap_near((float)iz, a.nz);
 }
 
 // S1xR2 with the (rho, z) correction table (StePS/src/forces.cc:1307-1350):
@@ -557,13 +567,20 @@ __global__ void __launch_bounds__(BLOCK) k_pair_s1tab(MixedArgs a)
             const float g2 = gx * gx + gy * gy + gz * gz;
             const bool full = wrapz || g2 <= bmax * bmax * 1.0001f + 1e-30f || coarse_for_gap(dOx, dOy, dOz, mI1, mJ1, g2, a.guard2);
 
+            // Far tile pairs of the continuous interpolants take the single-rounding
+            // separation, as the R^3 and T^3 kernels do; NGP picks a cell, so it
+            // keeps the double-float one everywhere.
+            const bool dfs = ORDER == 0 || full;
             float phx[IPT], phy[IPT], phz[IPT], plx[IPT], ply[IPT], plz[IPT];
-            float fx[IPT], fy[IPT], fz[IPT];
+            float px[IPT], py[IPT], pz[IPT], fx[IPT], fy[IPT], fz[IPT];
 #pragma unroll
             for (int k = 0; k < IPT; k++) {
                 frame_split(xi[k], lx[k], dOx, eOx, phx[k], plx[k]);
                 frame_split(yi[k], ly[k], dOy, eOy, phy[k], ply[k]);
                 frame_split(zi[k], lz[k], dOz, eOz, phz[k], plz[k]);
+                px[k] = phx[k] + plx[k];
+                py[k] = phy[k] + ply[k];
+                pz[k] = phz[k] + plz[k];
                 fx[k] = fy[k] = fz[k] = 0.0f;
             }
             const float4 *spb = sp[buf];
@@ -577,11 +594,19 @@ __global__ void __launch_bounds__(BLOCK) k_pair_s1tab(MixedArgs a)
 #pragma unroll
                 for (int k = 0; k < IPT; k++) {
                     const bool self = full && jid == ii[k];
-                    const float4 ql = sresb[jj];
-                    const float dx = self ? 0.0f : (q.x - phx[k]) + (ql.x - plx[k]);
-                    const float dy = self ? 0.0f : (q.y - phy[k]) + (ql.y - ply[k]);
-                    float dz = self ? 0.0f : (q.z - phz[k]) + (ql.z - plz[k]);
-                    if (wrapz && !self) dz = nearest_image(dz, q.z, phz[k], ql.z, plz[k], L, halfL, a.halfL_lo, a.wrap_tol);
+                    float dx, dy, dz;
+                    if (dfs) {
+                        const float4 ql = sresb[jj];
+                        dx = self ? 0.0f : (q.x - phx[k]) + (ql.x - plx[k]);
+                        dy = self ? 0.0f : (q.y - phy[k]) + (ql.y - ply[k]);
+                        dz = self ? 0.0f : (q.z - phz[k]) + (ql.z - plz[k]);
+                        if (wrapz && !self)
+                            dz = nearest_image(dz, q.z, phz[k], ql.z, plz[k], L, halfL, a.halfL_lo, a.wrap_tol);
+                    } else {
+                        dx = q.x - px[k];
+                        dy = q.y - py[k];
+                        dz = q.z - pz[k];
+                    }
                     const float rho2 = fmaf(dx, dx, dy * dy);
                     const float r2 = fmaf(dz, dz, rho2);
                     const float ri = rsqrt_mufu(r2);
@@ -594,23 +619,26 @@ __global__ void __launch_bounds__(BLOCK) k_pair_s1tab(MixedArgs a)
                     float Dr, Dz;
                     if (ORDER == 0) {
                         // NGP picks a cell, a hard decision: within FP32 rounding of
-                        // a cell face it is taken on the FP64 separation, with the
-                        // reference's own arithmetic (StePS/src/ewald_space.cc:803-840).
+                        // a cell face it is taken on the FP64 separation.
                         const float ur = fminf(fmaxf(rho, 0.0f), rho_max) * irho + 0.5f;
                         const float uzc = (dz + halfL) * iz;
-                        const float fr = ur - floorf(ur), fz = uzc - floorf(uzc);
+                        const float flr = floorf(ur), flz = floorf(uzc);
                         // FP32 (rho, z) carry < 3e-7 relative error; margin 2x
                         const float tr = 6e-7f * ur + 2e-6f, tz = 6e-7f * uzc + 2e-6f;
-                        int ir, izc;
-                        if (!self && (fr < tr || fr > 1.0f - tr || fz < tz || fz > 1.0f - tz)) {
-                            const double dx64 = exact_sep(q.x, phx[k], ql.x, plx[k]);
-                            const double dy64 = exact_sep(q.y, phy[k], ql.y, ply[k]);
-                            double dz64 = exact_sep(q.z, phz[k], ql.z, plz[k]);
-                            if (dz != (q.z - phz[k]) + (ql.z - plz[k])) dz64 -= copysign(a.s1_L, dz64);  // wrapped
-                            ngp_index_fp64(dx64, dy64, dz64, a, ir, izc);
-                        } else {
-                            ir = min(max((int)floorf(ur), 0), a.nrho - 1);
-                            izc = wrap_near(floorf(uzc), a.nz);
+                        int ir = min(max((int)flr, 0), a.nrho - 1);
+                        int izc = wrap_near(flz, a.nz);
+                        const bool amb_r = fabsf(ur - flr - 0.5f) > 0.5f - tr;
+                        const bool amb_z = fabsf(uzc - flz - 0.5f) > 0.5f - tz;
+                        if (!self && (amb_r || amb_z)) {
+                            const float4 ql = sresb[jj];
+                            if (amb_r)
+                                ir = ngp_rho_index(exact_sep(q.x, phx[k], ql.x, plx[k]),
+                                                   exact_sep(q.y, phy[k], ql.y, ply[k]), ur, a);
+                            if (amb_z) {
+                                double dz64 = exact_sep(q.z, phz[k], ql.z, plz[k]);
+                                if (dz != (q.z - phz[k]) + (ql.z - plz[k])) dz64 -= copysign(a.s1_L, dz64);  // wrapped
+                                izc = ngp_z_index(dz64, uzc, a);
+                            }
                         }
                         const float2 v = __ldg(tab + (size_t)ir * a.nz + izc);
                         Dr = v.x;
@@ -814,9 +842,8 @@ void s1tab_args(MixedArgs &a, const KParams &kp, const Tables &tb, cudaStream_t 
     a.irho = (float)(1.0 / drho);
     a.iz = (float)((double)tb.nz / kp.L);
     a.rho_max = (float)tb.rho_max;
-    a.s1_rho_max = tb.rho_max;
-    a.s1_idrho = drho > 0.0 ? 1.0 / drho : 0.0;
-    a.s1_idz = (double)tb.nz / kp.L;
+    a.s1_drho = drho;
+    a.s1_dzc = kp.L / (double)tb.nz;
     a.s1_L = kp.L;
 }
 

@@ -273,3 +273,44 @@ def test_s1r2_nearest_image_at_half_period(engine, mode):
     F64 = engine.forces(x, p, S.FP64)
     e = rel_err(engine.forces(x, p, S.MIXED), F64)
     assert np.percentile(e[:n // 2], 99) < MIXED_P99, np.percentile(e[:n // 2], [50, 99, 100])
+
+
+def test_s1r2_ngp_at_cell_faces(engine):
+    """NGP (order 0) picks a table cell, a hard decision. Pairs are planted
+    with their (rho, z) separation within +-4e-7 (relative) of a cell face:
+    rho = (K - 1/2) drho, or dz + L/2 = K dz_cell. At these offsets FP32
+    rounding alone takes the wrong cell for about 6 % (rho) and 14 % (z) of
+    the pairs. A wrong cell moves the pair force by ~1e-3 relative, so the
+    mixed kernel must take these decisions on the FP64 separation."""
+    g = golden("s1r2_table_o0")
+    nrho, nz = (int(v) for v in g["shape"])
+    L, rsim = float(g["L"]), float(g["rsim"])
+    drho, dzc = 2.25 * rsim / (nrho - 1), L / nz
+    rng = np.random.default_rng(17)
+    npair = 384
+    base = np.column_stack([rng.uniform(-300, 300, npair), rng.uniform(-300, 300, npair), rng.uniform(0, L, npair)])
+    kind = np.arange(npair) % 3  # 0: rho face, 1: z face, 2: both
+    K = rng.integers(1, 24, npair)
+    rho = np.where(kind != 1, (K - 0.5) * drho * (1 + rng.uniform(-4e-7, 4e-7, npair)),
+                   (rng.integers(1, 24, npair) + rng.uniform(-0.3, 0.3, npair)) * drho)
+    Kz = rng.integers(nz // 4, 3 * nz // 4 + 1, npair)
+    dz = np.where(kind != 0, Kz * dzc - L / 2 + L * rng.uniform(-4e-7, 4e-7, npair),
+                  (rng.integers(nz // 4, 3 * nz // 4, npair) + 0.5 + rng.uniform(-0.3, 0.3, npair)) * dzc - L / 2)
+    phi = rng.uniform(0, 2 * np.pi, npair)
+    sep = np.column_stack([rho * np.cos(phi), rho * np.sin(phi), dz])
+    x = np.empty((2 * npair, 3))
+    x[0::2], x[1::2] = base, base + sep
+    x[:, 2] %= L
+    m = np.ones(2 * npair)
+    eps = np.full(2 * npair, 0.05)
+    engine.set_particles(m, eps)
+    engine.set_table_s1r2(g["table"], nrho, nz)
+    p = s1_params(g, 2, images=0, order=0)
+    F64 = engine.forces(x, p, S.FP64)
+    for threads, ipt in ((128, 1), (64, 2)):
+        engine.set_tuning(threads, ipt, 0)
+        try:
+            e = rel_err(engine.forces(x, p, S.MIXED), F64)
+        finally:
+            engine.set_tuning(128, 2, 0)
+        assert e.max() < 1e-4 and np.percentile(e, 99) < MIXED_P99, (threads, ipt, np.percentile(e, [50, 99, 100]))
