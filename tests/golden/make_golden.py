@@ -7,7 +7,8 @@ pin: tests/test_golden.py checks the plain-C oracle against them on any
 machine, and the GPU tests check the CUDA kernels against them.
 
 Run from the repository root:  python tests/golden/make_golden.py
-(``... make_golden.py fp32`` regenerates only the single-precision floor).
+(``... make_golden.py fp32`` regenerates only the single-precision floor,
+``... make_golden.py background`` only the S1xR2 background-term vectors).
 """
 from __future__ import annotations
 
@@ -153,6 +154,34 @@ def main():
     save("softening", r=rs, w_beta1=w, w_beta037=w2)
 
 
+def s1_background():
+    """The S1xR2 background terms the other vectors leave out, on the inputs of
+    s1r2_images.npz: the comoving term with the radial correction at
+    IS_PERIODIC = 1 (StePS/src/forces.cc:1383-1390), the non-comoving H0^2
+    Omega_L x term (forces.cc:1298-1303), and the table mode's plain
+    mass_in_unit_sphere x (forces.cc:1340-1344) with its H0^2 Omega_L twin."""
+    g = np.load(os.path.join(HERE, "s1r2_images.npz"))
+    t = np.load(os.path.join(HERE, "s1r2_table_o2.npz"))
+    mius, h0, oml = 0.011, 0.07, 0.69
+    ref = O.Ref("s1nl")
+    ref.set_particles(g["x"], g["m"], g["eps"])
+    ref.set_radial_table(g["radial"])
+    ref.set_params(is_periodic=1, L=S1_LZ, rsim=S1_RSIM, cosmology=1, comoving=1, mius=mius)
+    F_is1_comoving = ref.forces()
+    ref.set_params(is_periodic=2, L=S1_LZ, rsim=S1_RSIM, cosmology=1, comoving=0, h0=h0, oml=oml)
+    F_is2_de = ref.forces()
+    ref = O.Ref("s1o2")
+    ref.set_particles(t["x"], t["m"], t["eps"])
+    ref.set_s1r2_table(t["table"], S1_NRHO, S1_NZ)
+    ref.set_radial_table(g["radial"])
+    ref.set_params(is_periodic=2, L=S1_LZ, rsim=S1_RSIM, cosmology=1, comoving=1, mius=mius)
+    F_table_comoving = ref.forces()
+    ref.set_params(is_periodic=2, L=S1_LZ, rsim=S1_RSIM, cosmology=1, comoving=0, h0=h0, oml=oml)
+    F_table_de = ref.forces()
+    save("s1r2_background", mius=np.array(mius), h0=np.array(h0), oml=np.array(oml), F_is1_comoving=F_is1_comoving,
+         F_is2_de=F_is2_de, F_table_comoving=F_table_comoving, F_table_de=F_table_de)
+
+
 def fp32_floor():
     """The reference's own single-precision build (USE_SINGLE_PRECISION) on the
     same inputs as its FP64 build: the error floor of the reference's FP32 path
@@ -186,6 +215,9 @@ def fp32_floor():
 if __name__ == "__main__":
     if sys.argv[1:] == ["fp32"]:
         fp32_floor()
+    elif sys.argv[1:] == ["background"]:
+        s1_background()
     else:
         main()
         fp32_floor()
+        s1_background()

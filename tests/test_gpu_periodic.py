@@ -45,6 +45,26 @@ def test_s1r2_images_mixed(engine):
     assert err_stats(engine.forces(g["x"], p, S.MIXED), g["F_comoving"])["p99"] < MIXED_P99
 
 
+@pytest.mark.parametrize("key", ["F_is1_comoving", "F_is2_de", "F_table_comoving", "F_table_de"])
+def test_s1r2_background_terms(engine, key):
+    """Comoving with the radial correction at IS_PERIODIC = 1, non-comoving
+    H0^2 Omega_L x (image sum and table), and the table mode's plain
+    mass_in_unit_sphere x, against the reference's golden vectors."""
+    g, b, t = golden("s1r2_images"), golden("s1r2_background"), golden("s1r2_table_o2")
+    cosmo = dict(cosmology=1, comoving=1, mius=float(b["mius"])) if key.endswith("comoving") else \
+        dict(cosmology=1, comoving=0, h0=float(b["h0"]), oml=float(b["oml"]))
+    engine.set_particles(g["m"], g["eps"])
+    engine.set_radial_table(g["radial"])
+    if key.startswith("F_table"):
+        nrho, nz = (int(v) for v in t["shape"])
+        engine.set_table_s1r2(t["table"], nrho, nz)
+        p = s1_params(g, 2, images=0, order=2, **cosmo)
+    else:
+        p = s1_params(g, 1 if key == "F_is1_comoving" else 2, **cosmo)
+    assert rel_err(engine.forces(g["x"], p, S.FP64), b[key]).max() < FP64_TOL
+    assert err_stats(engine.forces(g["x"], p, S.MIXED), b[key])["p99"] < MIXED_P99
+
+
 @pytest.mark.parametrize("isp", [3, 15])
 def test_s1r2_other_image_counts(engine, port, isp):
     ps = W.s1r2_cylindrical(3000, 200.0, 600.0, seed=20 + isp)

@@ -118,6 +118,27 @@ def test_s1r2_table(port, order):
     assert rel_err(port.forces(s, g["x"]), g["F"]).max() < TOL
 
 
+def test_s1r2_background_terms(port):
+    """The S1xR2 background terms: comoving with the radial correction at
+    IS_PERIODIC = 1, non-comoving H0^2 Omega_L x, and the table mode's plain
+    mass_in_unit_sphere x."""
+    g, b, t = golden("s1r2_images"), golden("s1r2_background"), golden("s1r2_table_o2")
+    L, rsim = float(g["L"]), float(g["rsim"])
+    mius, h0, oml = float(b["mius"]), float(b["h0"]), float(b["oml"])
+    nrho, nz = (int(v) for v in t["shape"])
+    cases = [
+        (3, dict(is_periodic=1, cosmology=1, comoving=1, mius=mius), {}, "F_is1_comoving"),
+        (3, dict(is_periodic=2, cosmology=1, comoving=0, h0=h0, oml=oml), {}, "F_is2_de"),
+        (2, dict(is_periodic=2, cosmology=1, comoving=1, mius=mius), dict(table=t["table"], nrho=nrho, nz=nz, order=2),
+         "F_table_comoving"),
+        (2, dict(is_periodic=2, cosmology=1, comoving=0, h0=h0, oml=oml),
+         dict(table=t["table"], nrho=nrho, nz=nz, order=2), "F_table_de"),
+    ]
+    for topo, pkw, skw, key in cases:
+        s = port.system(topo, g["m"], g["eps"], port_params(O, L=L, rsim=rsim, **pkw), radial=g["radial"], **skw)
+        assert rel_err(port.forces(s, g["x"]), b[key]).max() < TOL, key
+
+
 def test_two_body_analytic(port):
     # Beyond the softening support the pair force is Newton's m / r^2.
     x = np.array([[0.0, 0.0, 0.0], [3.0, 4.0, 0.0]])
