@@ -144,7 +144,13 @@ int steps_gpu_forces(const steps_params *p, int precision, const double *x, doub
  * stays on the device until steps_gpu_download_forces. No host copies. */
 int steps_gpu_upload_positions(const double *x);
 int steps_gpu_forces_resident(const steps_params *p, int precision, int id_min, int id_max);
+/* Copies the forces of the last successful force call (any entry point of
+ * this context, the KDK steps included) into F, double[3 * count] with count
+ * from steps_gpu_forces_range. New masses (steps_gpu_set_particles) and a
+ * failed force call leave no range: STEPS_E_STATE. */
 int steps_gpu_download_forces(double *F);
+/* The i range the resident forces cover: *id_min and *count (0 when none). */
+int steps_gpu_forces_range(int *id_min, int *count);
 
 /* ---- leapfrog (device resident) ----------------------------------------- */
 

@@ -124,11 +124,19 @@ class Engine:
         if id_max is None:
             id_max = self.n - 1
         self._check(self.lib.steps_gpu_forces_resident(C.byref(p), int(precision), int(id_min), int(id_max)))
-        self._last_ni = id_max - id_min + 1
+
+    def forces_range(self):
+        """(id_min, count) of the resident forces; count 0 when there are none."""
+        lo, cnt = C.c_int(0), C.c_int(0)
+        self._check(self.lib.steps_gpu_forces_range(C.byref(lo), C.byref(cnt)))
+        return lo.value, cnt.value
 
     def download_forces(self, ni=None) -> np.ndarray:
-        ni = ni or self._last_ni
-        F = np.empty((ni, 3))
+        # The library copies the whole range of the last force call.
+        _, cnt = self.forces_range()
+        if ni is not None and ni != cnt:
+            raise ValueError(f"the resident forces cover {cnt} particles, not {ni}")
+        F = np.empty((max(cnt, 1), 3))
         self._check(self.lib.steps_gpu_download_forces(_d(F)))
         return F
 

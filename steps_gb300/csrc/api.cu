@@ -146,6 +146,9 @@ void compute_forces(const steps_params *p, int precision, int id_min, int id_max
     KParams kp = derive_params(p);
     Tables tb = device_tables(kp);
     int ni = id_max - id_min + 1;
+    // Until this call succeeds the force buffer holds no valid range.
+    c.F_ni = 0;
+    c.F_valid = false;
     double *F = c.F.ensure<double>(3 * (size_t)c.n);
     if (precision == STEPS_FP64)
         forces_fp64(kp, tb, c.x.as<double>(), c.n, id_min, ni, F);
@@ -242,9 +245,13 @@ int steps_gpu_set_particles(int n, const double *m, const double *eps)
         if (n <= 0 || !m || !eps) fail(STEPS_E_ARG, "set_particles: n must be > 0 and m, eps non-NULL");
         if (n > (1 << 30)) fail(STEPS_E_ARG, "set_particles: n too large");
         if (n != c.n) {
-            c.have_x = c.have_v = c.F_valid = false;
+            c.have_x = c.have_v = false;
             c.tj.ordered = c.ti.ordered = false;
         }
+        // New masses or softening make the last forces stale, and a smaller n
+        // must not let steps_gpu_download_forces copy the old, longer range.
+        c.F_valid = false;
+        c.F_lo = c.F_ni = 0;
         STEPS_CUDA(cudaMemcpyAsync(c.m64.ensure<double>(n), m, sizeof(double) * n, cudaMemcpyHostToDevice, c.stream));
         STEPS_CUDA(cudaMemcpyAsync(c.eps64.ensure<double>(n), eps, sizeof(double) * n, cudaMemcpyHostToDevice, c.stream));
         STEPS_CUDA(cudaStreamSynchronize(c.stream));
@@ -293,6 +300,15 @@ int steps_gpu_download_forces(double *F)
         if (c.F_ni <= 0) fail(STEPS_E_STATE, "no forces computed");
         STEPS_CUDA(cudaMemcpyAsync(F, c.F.as<double>(), sizeof(double) * 3 * c.F_ni, cudaMemcpyDeviceToHost, c.stream));
         STEPS_CUDA(cudaStreamSynchronize(c.stream));
+    });
+}
+
+int steps_gpu_forces_range(int *id_min, int *count)
+{
+    return guarded([&] {
+        if (!id_min || !count) fail(STEPS_E_ARG, "id_min and count must be non-NULL");
+        *id_min = g_ctx.F_lo;
+        *count = g_ctx.F_ni;
     });
 }
 

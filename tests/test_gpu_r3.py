@@ -186,6 +186,35 @@ def test_errors(engine):
     assert rel_err(engine.forces(g["x"], S.params(S.R3), S.FP64), g["F"]).max() < FP64_TOL
 
 
+def test_resident_forces_range(engine):
+    """steps_gpu_download_forces copies the range of the last successful force
+    call. New masses leave none, so a caller that shrinks n cannot be handed the
+    old, longer range; a call refused by argument checks keeps the range (a
+    call that fails while running clears it: tests/test_gpu_timeout.py)."""
+    g = golden("r3_n2048")
+    p = S.params(S.R3)
+    engine.set_particles(g["m"], g["eps"])
+    engine.upload_positions(g["x"])
+    engine.forces_resident(p, S.FP64, 100, 611)
+    assert engine.forces_range() == (100, 512)
+    assert rel_err(engine.download_forces(512), g["F"][100:612]).max() < FP64_TOL
+    engine.set_particles(g["m"][:16], g["eps"][:16])
+    assert engine.forces_range() == (0, 0)
+    with pytest.raises(S.StepsError) as e:
+        engine.download_forces()
+    assert e.value.code == S.STEPS_E_STATE
+    engine.set_particles(g["m"], g["eps"])
+    engine.upload_positions(g["x"])
+    engine.forces_resident(p, S.FP64)
+    assert engine.forces_range() == (0, 2048)
+    with pytest.raises(S.StepsError):
+        engine.forces_resident(p, 7)
+    assert engine.forces_range() == (0, 2048)  # refused before any work: the range stands
+    with pytest.raises(S.StepsError):
+        engine.forces_resident(p, S.FP64, 0, 4096)
+    assert engine.forces_range() == (0, 2048)
+
+
 def test_page_locked_host_buffers(engine):
     """steps_gpu_host_alloc memory works as the host buffers of the drop-in
     call and gives bit-identical results to ordinary host memory."""

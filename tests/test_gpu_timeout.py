@@ -25,6 +25,7 @@ def test_pipeline_wait_runs_out_and_reports(engine):
             engine.forces(g["x"], p, S.MIXED)
         assert e.value.code == S.STEPS_E_TIMEOUT
         assert time.time() - t0 < 30
+        assert engine.forces_range() == (0, 0)  # no forces left from the failed call
         # the hook is one shot and the context is intact
         F = engine.forces(g["x"], p, S.MIXED)
         assert err_stats(F, g["F"])["p99"] < 1e-5
