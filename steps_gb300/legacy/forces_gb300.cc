@@ -23,6 +23,7 @@
  * Precision: STEPS_GB300_PRECISION=fp64|mixed in the environment, default
  * mixed (FP32 pair arithmetic, FP64 accumulation, p99 error <= 1e-5).
  */
+#include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -210,11 +211,12 @@ extern "C" void steps_gb300_legacy_precision(int precision)
     }
 }
 
-/* forces.cc:43-50 */
+/* forces.cc:43-50: the same expression (pow, and pi rounded to the same
+ * double), so rho_part -- and with it step.cc's errmax -- is bit-identical. */
 void recalculate_softening()
 {
     beta = ParticleRadi;
-    if (COSMOLOGY == 1) rho_part = M_min / (4.0 * 3.14159265358979323846 * beta * beta * beta / 3.0);
+    if (COSMOLOGY == 1) rho_part = M_min / (4.0 * 3.14159265358979323846 * pow(beta, 3.0) / 3.0);
 }
 
 #if !defined(PERIODIC) && !defined(PERIODIC_Z)

@@ -33,6 +33,7 @@ REAL *RADIAL_FORCE_TABLE;
 void forces(REAL *x, REAL *F, int ID_min, int ID_max);
 void forces_periodic(REAL *x, REAL *F, int ID_min, int ID_max);
 void forces_periodic_z(REAL *x, REAL *F, int ID_min, int ID_max);
+void recalculate_softening();
 extern "C" void steps_gb300_legacy_precision(int precision);
 
 extern "C" {
@@ -68,6 +69,18 @@ void h_table(const double *t, int a, int b)
 #endif
 }
 void h_precision(int p) { steps_gb300_legacy_precision(p); }
+// Sets the globals recalculate_softening reads, calls it, returns beta and
+// rho_part (host only: no GPU context is created).
+void h_softening(double radius, double m_min, int cosmology, double *beta_out, double *rho_out)
+{
+    ParticleRadi = radius;
+    M_min = m_min;
+    COSMOLOGY = cosmology;
+    rho_part = 0;
+    recalculate_softening();
+    *beta_out = beta;
+    *rho_out = rho_part;
+}
 int h_forces(double *x, double *F, int id_min, int id_max)
 {
     ForceError = false;
