@@ -135,6 +135,8 @@ int steps_gpu_set_radial_table(int size, const double *table);
 /* The drop-in force call with HOST buffers: uploads x (double[3n]), computes
  * the accelerations of particles id_min..id_max against all n particles and
  * downloads them into F (double[3*(id_max-id_min+1)], overwritten).
+ * id_max = id_min - 1 is the empty range: nothing is computed or written (F
+ * may then be NULL), as the reference's loop over an empty range does.
  * Equivalent of forces()/forces_periodic()/forces_periodic_z()
  * (forces.cc:510/776/1221, forces_cuda.cu:878/1121/1378). */
 int steps_gpu_forces(const steps_params *p, int precision, const double *x, double *F, int id_min, int id_max);

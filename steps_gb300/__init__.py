@@ -107,8 +107,9 @@ class Engine:
         x = np.ascontiguousarray(x, dtype=np.float64)
         if id_max is None:
             id_max = self.n - 1
-        F = np.empty((id_max - id_min + 1, 3)) if out is None else out
-        assert F.shape == (id_max - id_min + 1, 3) and F.dtype == np.float64 and F.flags.c_contiguous
+        ni = max(id_max - id_min + 1, 0)  # the library checks the range itself
+        F = np.empty((ni, 3)) if out is None else out
+        assert F.shape == (ni, 3) and F.dtype == np.float64 and F.flags.c_contiguous
         self._check(self.lib.steps_gpu_forces(C.byref(p), int(precision), _d(x), _d(F), int(id_min), int(id_max)))
         return F
 

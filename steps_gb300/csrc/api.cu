@@ -141,7 +141,10 @@ void compute_forces(const steps_params *p, int precision, int id_min, int id_max
     require_init();
     if (c.n <= 0) fail(STEPS_E_STATE, "no particles: call steps_gpu_set_particles first");
     if (!c.have_x) fail(STEPS_E_STATE, "no positions uploaded");
-    if (id_min < 0 || id_max >= c.n || id_max < id_min) fail(STEPS_E_ARG, "i range outside [0, n)");
+    // id_max = id_min - 1 is the empty range: no work, as in the reference's
+    // loop over [ID_min, ID_max] (StePS/src/forces.cc:520-556).
+    if (id_min < 0 || id_min > c.n || id_max >= c.n || id_max < id_min - 1)
+        fail(STEPS_E_ARG, "i range outside [0, n)");
     if (precision != STEPS_FP64 && precision != STEPS_MIXED) fail(STEPS_E_ARG, "unknown precision mode");
     KParams kp = derive_params(p);
     Tables tb = device_tables(kp);
@@ -149,6 +152,10 @@ void compute_forces(const steps_params *p, int precision, int id_min, int id_max
     // Until this call succeeds the force buffer holds no valid range.
     c.F_ni = 0;
     c.F_valid = false;
+    if (ni == 0) {
+        c.F_lo = id_min;
+        return;
+    }
     double *F = c.F.ensure<double>(3 * (size_t)c.n);
     if (precision == STEPS_FP64)
         forces_fp64(kp, tb, c.x.as<double>(), c.n, id_min, ni, F);
@@ -317,15 +324,16 @@ int steps_gpu_forces(const steps_params *p, int precision, const double *x, doub
     return guarded([&] {
         require_init();
         Ctx &c = g_ctx;
-        if (!x || !F) fail(STEPS_E_ARG, "x and F must be non-NULL");
+        if (!x || (!F && id_max >= id_min)) fail(STEPS_E_ARG, "x and F must be non-NULL");
         if (c.n <= 0) fail(STEPS_E_STATE, "no particles: call steps_gpu_set_particles first");
         STEPS_CUDA(cudaMemcpyAsync(c.x.ensure<double>(3 * (size_t)c.n), x, sizeof(double) * 3 * c.n,
                                    cudaMemcpyHostToDevice, c.stream));
         c.have_x = true;
         compute_forces(p, precision, id_min, id_max, false);
         int ni = id_max - id_min + 1;
-        STEPS_CUDA(cudaMemcpyAsync(F, c.F.as<double>(), sizeof(double) * 3 * (size_t)ni, cudaMemcpyDeviceToHost,
-                                   c.stream));
+        if (ni > 0)
+            STEPS_CUDA(cudaMemcpyAsync(F, c.F.as<double>(), sizeof(double) * 3 * (size_t)ni, cudaMemcpyDeviceToHost,
+                                       c.stream));
         STEPS_CUDA(cudaStreamSynchronize(c.stream));
     });
 }

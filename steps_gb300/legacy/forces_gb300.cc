@@ -151,6 +151,7 @@ int set_s1(int nrho, int nz, const double *t) { return steps_gpu_set_table_s1r2(
 
 void run(const steps_params &p, REAL *x, REAL *F, int ID_min, int ID_max)
 {
+    if (ID_max < ID_min) return;  // an empty range: the reference's loops do nothing (forces.cc:520-556)
     if (!ensure_context() || !sync_particles()) return;
     int ni = ID_max - ID_min + 1;
     const double *xd;

@@ -77,6 +77,12 @@ def test_forces_r3(tmp_path_factory, engine):
     # a bad i range sets ForceError instead of aborting
     rc, F = run(h, g["x"], 0, 10, 5000)
     assert rc == 1
+    # an empty range (an MPI rank with no particles) is no work and no error
+    x = np.ascontiguousarray(g["x"])
+    F = np.zeros((1, 3))
+    for lo, hi in ((10, 9), (10, 3)):
+        assert h.h_forces(x.ctypes.data_as(_dp), F.ctypes.data_as(_dp), lo, hi) == 0
+    assert not F.any()
 
 
 def test_forces_periodic_t3(tmp_path_factory, engine):

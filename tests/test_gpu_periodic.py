@@ -334,3 +334,66 @@ def test_s1r2_ngp_at_cell_faces(engine):
         finally:
             engine.set_tuning(128, 2, 0)
         assert e.max() < 1e-4 and np.percentile(e, 99) < MIXED_P99, (threads, ipt, np.percentile(e, [50, 99, 100]))
+
+
+MODES = ["t3_o2", "t3_o4", "s1_images", "s1_table_o0", "s1_table_o2", "s1_table_o4"]
+
+
+def _mode_setup(engine, mode, n):
+    """The first n particles of the mode's golden set, the golden table
+    uploaded, and (library params, oracle system factory)."""
+    if mode.startswith("t3"):
+        order = int(mode[-1])
+        g = golden(f"t3_o{order}")
+        ng, L = int(g["ngrid"]), float(g["L"])
+        engine.set_table_t3(g["table"], ng)
+        p = S.params(S.T3, is_periodic=2, L=L, rsim=L / 2, ewald_order=order)
+        sysf = lambda port, m, e: port.system(1, m, e, port_params(O, is_periodic=2, L=L, rsim=L / 2),  # noqa: E731
+                                              table=g["table"], ngrid=ng, order=order)
+    elif mode == "s1_images":
+        g = golden("s1r2_images")
+        L, rsim = float(g["L"]), float(g["rsim"])
+        p = s1_params(g, 2)
+        sysf = lambda port, m, e: port.system(3, m, e, port_params(O, is_periodic=2, L=L, rsim=rsim))  # noqa: E731
+    else:
+        order = int(mode[-1])
+        g = golden(f"s1r2_table_o{order}")
+        L, rsim = float(g["L"]), float(g["rsim"])
+        nrho, nz = (int(v) for v in g["shape"])
+        engine.set_table_s1r2(g["table"], nrho, nz)
+        p = s1_params(g, 2, images=0, order=order)
+        sysf = lambda port, m, e: port.system(2, m, e, port_params(O, is_periodic=2, L=L, rsim=rsim),  # noqa: E731
+                                              table=g["table"], nrho=nrho, nz=nz, order=order)
+    x, m, eps = g["x"][:n], g["m"][:n], g["eps"][:n]
+    engine.set_particles(m, eps)
+    return x, m, eps, p, sysf, float(g["L"])
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 129, 1000])
+@pytest.mark.parametrize("mode", MODES)
+def test_periodic_edge_sizes(engine, port, mode, n):
+    """Tiny and ragged particle counts (one particle, a pair, partial tiles)
+    in every periodic mode: FP64 against the oracle to 1e-12, mixed against
+    FP64, and single-particle i ranges at both ends. A lone particle's force
+    (its own images and table correction) is ~0, so forces below 1e-9 of the
+    set's scale m_total / L^2 are compared in absolute terms."""
+    x, m, eps, p, sysf, L = _mode_setup(engine, mode, n)
+    Fo = port.forces(sysf(port, m, eps), x)
+    scale = float(m.sum()) / L ** 2
+    big = np.linalg.norm(Fo, axis=1) > 1e-9 * scale
+
+    def check(F, Fref, sel, tol_rel, tol_abs):
+        assert np.abs(F[~sel] - Fref[~sel]).max(initial=0.0) <= tol_abs * scale
+        if sel.any():
+            e = rel_err(F[sel], Fref[sel])
+            assert (e.max() if tol_rel == FP64_TOL else np.percentile(e, 99)) < tol_rel, np.percentile(e, [50, 99, 100])
+
+    F64 = engine.forces(x, p, S.FP64)
+    check(F64, Fo, big, FP64_TOL, 1e-12)
+    Fm = engine.forces(x, p, S.MIXED)
+    check(Fm, F64, big, MIXED_P99, 1e-6)
+    for lo in {0, n - 1}:
+        Fl = engine.forces(x, p, S.FP64, lo, lo)
+        check(Fl, Fo[lo:lo + 1], big[lo:lo + 1], FP64_TOL, 1e-12)
+        Fl = engine.forces(x, p, S.MIXED, lo, lo)
+        check(Fl, Fo[lo:lo + 1], big[lo:lo + 1], 1e-4, 1e-6)

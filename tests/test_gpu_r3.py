@@ -4,6 +4,8 @@ against the reference's golden vectors and the plain-C oracle.
 Tolerances: the plain FP64 kernel must match the reference FP64 CPU path to
 1e-12 relative per particle; the mixed kernel (FP32 pairs, FP64
 accumulation) must have p99 relative error <= 1e-5 against FP64."""
+import ctypes as C
+
 import numpy as np
 import pyoracle as O
 import pytest
@@ -171,7 +173,10 @@ def test_errors(engine):
     g = golden("r3_n2048")
     engine.set_particles(g["m"], g["eps"])
     with pytest.raises(S.StepsError) as e:
-        engine.forces(g["x"], S.params(S.R3), S.FP64, 5, 4)
+        engine.forces(g["x"], S.params(S.R3), S.FP64, 5, 3)
+    assert e.value.code == S.STEPS_E_ARG
+    with pytest.raises(S.StepsError) as e:
+        engine.forces(g["x"], S.params(S.R3), S.FP64, g["m"].size + 1, g["m"].size)
     assert e.value.code == S.STEPS_E_ARG
     with pytest.raises(S.StepsError) as e:
         engine.forces(g["x"], S.params(S.R3), S.FP64, 0, g["m"].size)
@@ -183,6 +188,23 @@ def test_errors(engine):
         engine.set_tuning(96, 3)
     assert e.value.code == S.STEPS_E_ARG
     # the context stays usable after errors
+    assert rel_err(engine.forces(g["x"], S.params(S.R3), S.FP64), g["F"]).max() < FP64_TOL
+
+
+@pytest.mark.parametrize("lo", [0, 5, 2048])
+def test_empty_range(engine, lo):
+    """id_max = id_min - 1 is an empty range: no work and no error, as the
+    reference's loop over [ID_min, ID_max] does nothing; the next call is
+    unaffected."""
+    g = golden("r3_n2048")
+    engine.set_particles(g["m"], g["eps"])
+    for prec in (S.FP64, S.MIXED):
+        F = engine.forces(g["x"], S.params(S.R3), prec, lo, lo - 1)
+        assert F.shape == (0, 3)
+        assert engine.forces_range() == (lo, 0)
+    rc = engine.lib.steps_gpu_forces(C.byref(S.params(S.R3)), S.FP64, g["x"].ctypes.data_as(C.POINTER(C.c_double)),
+                                     None, lo, lo - 1)
+    assert rc == S.STEPS_OK
     assert rel_err(engine.forces(g["x"], S.params(S.R3), S.FP64), g["F"]).max() < FP64_TOL
 
 
