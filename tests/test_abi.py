@@ -48,3 +48,15 @@ def test_calls_without_init_fail_cleanly(lib):
     assert rc == S.STEPS_E_STATE
     assert b"steps_gpu_init" in lib.steps_gpu_error_string()
     assert lib.steps_gpu_abi_version() == 1
+
+
+def test_missing_library_fails_loudly(tmp_path):
+    """No CPU fallback: without the built library the package raises."""
+    import steps_gb300 as S
+
+    loaded, S._LIB = S._LIB, None
+    try:
+        with pytest.raises(RuntimeError, match="is missing"):
+            S.load_library(str(tmp_path / "libsteps_gb300.so"))
+    finally:
+        S._LIB = loaded
