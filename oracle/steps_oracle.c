@@ -6,7 +6,8 @@
  * spline, sequential-in-j accumulation per i, OpenMP over i with per-pair
  * atomic adds as forces.cc:550-555 does) so that it is both a tight numerical
  * pin and a like-for-like CPU timing baseline. Pinned against the reference
- * compiled from source (oracle/_ref) by tests/test_oracle_pin.py.
+ * compiled from source (oracle/_ref) by tests/test_oracle_ref.py, and against
+ * the golden vectors it produced by tests/test_oracle_golden.py.
  *
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load
  * this library; the product library never does.

@@ -7,7 +7,8 @@
  *
  * Parity is pinned against the UNMODIFIED reference CPU sources compiled
  * from the reference tree (oracle/_ref, see oracle/Makefile) by
- * tests/test_oracle_pin.py and against the golden vectors in tests/golden/.
+ * tests/test_oracle_ref.py and against the golden vectors in tests/golden/
+ * by tests/test_oracle_golden.py.
  *
  * All arrays are AoS: x[3*i+k]; forces are accelerations with G = 1,
  * overwritten (not accumulated) for i in [id_min, id_max], stored at

@@ -3,7 +3,7 @@ reference StePS CPU force path, compiled from the reference tree into
 oracle/_ref (``make -C oracle ref``), on small seeded inputs.
 
 The reference has no tests or fixtures of its own, so these vectors are the
-pin: tests/test_golden.py checks the plain-C oracle against them on any
+pin: tests/test_oracle_golden.py checks the plain-C oracle against them on any
 machine, and the GPU tests check the CUDA kernels against them.
 
 Run from the repository root:  python tests/golden/make_golden.py

@@ -1,0 +1,87 @@
+"""The plain-C oracle against the reference's own CPU force path, compiled
+unmodified from the reference tree into oracle/_ref, on fresh seeded inputs
+(other seeds, sizes and i ranges than the golden vectors): R^3 with its three
+background modes, T^3 at orders 2 and 4 and nearest image, S1xR2 image sums
+at three IS_PERIODIC values and the (rho, z) table at orders 0/2/4, and both
+table builders at other grid sizes. Runs where the reference build exists
+(it does not travel to machines without the reference tree)."""
+import math
+
+import numpy as np
+import pyoracle as O
+import pytest
+
+from helpers import golden, port_params, rel_err
+from steps_gb300 import workloads as W
+
+pytestmark = pytest.mark.skipif(not all(O.ref_available(v) for v in ("r3", "t3o2", "t3o4", "s1nl", "s1o0")),
+                                reason="reference build (oracle/_ref) not present")
+
+TOL = 1e-13
+
+
+def _ref(variant, ps, **params):
+    ref = O.Ref(variant)
+    ref.set_particles(ps.x, ps.m, ps.eps)
+    ref.set_params(**params)
+    return ref
+
+
+@pytest.mark.parametrize("bg", ["none", "comoving", "de"])
+def test_r3(port, bg):
+    ps = W.r3_compactified(3001, 700.0, seed=301, displace=True)
+    kw = {"none": {}, "comoving": dict(cosmology=1, comoving=1, mius=0.23),
+          "de": dict(cosmology=1, comoving=0, h0=0.068, oml=0.7)}[bg]
+    ref = _ref("r3", ps, **kw)
+    s = port.system(0, ps.m, ps.eps, port_params(O, **kw))
+    for lo, hi in ((0, 3000), (17, 2900), (3000, 3000)):
+        # same operations in the same order: bit-identical
+        assert np.array_equal(port.forces(s, ps.x, lo, hi), ref.forces(lo, hi)), (lo, hi)
+
+
+@pytest.mark.parametrize("order", [2, 4])
+@pytest.mark.parametrize("isp", [1, 2])
+def test_t3(port, order, isp):
+    g = golden(f"t3_o{order}")
+    ng, L = int(g["ngrid"]), float(g["L"])
+    ps = W.t3_clumpy(1777, L, seed=302, n_clumps=9)
+    ref = _ref(f"t3o{order}", ps, is_periodic=isp, L=L, rsim=L / 2)
+    ref.set_t3_table(g["table"], ng)
+    s = port.system(1, ps.m, ps.eps, port_params(O, is_periodic=isp, L=L, rsim=L / 2), table=g["table"], ngrid=ng,
+                    order=order)
+    for lo, hi in ((0, 1776), (5, 1000)):
+        assert rel_err(port.forces(s, ps.x, lo, hi), ref.forces(lo, hi)).max() < TOL, (lo, hi)
+
+
+@pytest.mark.parametrize("isp", [1, 2, 3])
+def test_s1r2_images(port, isp):
+    ps = W.s1r2_cylindrical(1500, 150.0, 450.0, seed=303)
+    ref = _ref("s1nl", ps, is_periodic=isp, L=150.0, rsim=450.0)
+    s = port.system(3, ps.m, ps.eps, port_params(O, is_periodic=isp, L=150.0, rsim=450.0))
+    assert rel_err(port.forces(s, ps.x), ref.forces()).max() < TOL
+
+
+@pytest.mark.parametrize("order", [0, 2, 4])
+def test_s1r2_table(port, order):
+    g = golden(f"s1r2_table_o{order}")
+    nrho, nz = (int(v) for v in g["shape"])
+    L, rsim = float(g["L"]), float(g["rsim"])
+    ps = W.s1r2_cylindrical(1500, L, rsim, seed=304)
+    ref = _ref(f"s1o{order}", ps, is_periodic=2, L=L, rsim=rsim)
+    ref.set_s1r2_table(g["table"], nrho, nz)
+    s = port.system(2, ps.m, ps.eps, port_params(O, is_periodic=2, L=L, rsim=rsim), table=g["table"], nrho=nrho,
+                    nz=nz, order=order)
+    assert rel_err(port.forces(s, ps.x), ref.forces()).max() < TOL
+
+
+def test_table_builders_other_sizes(port):
+    """Both Ewald table builders at grid sizes the golden set does not use."""
+    L = 80.0
+    args = (2.0 / L, 2.0, 5.0 * 2.0 * math.pi / L, 3.0, 6.0)
+    want = O.Ref("t3o2").build_t3_table(19, L, *args)
+    got = port.t3_table(19, L, *args)
+    np.testing.assert_allclose(got, want, rtol=0, atol=1e-13 * np.abs(want).max())
+    lz, rmax = 120.0, 2.25 * 300.0
+    want = O.Ref("s1o2").build_s1r2_table(40, 12, rmax, lz, 0.787875 / lz, 4, 10)
+    got = port.s1r2_table(40, 12, rmax, lz, 0.787875 / lz, 4, 10)
+    np.testing.assert_allclose(got, want, rtol=0, atol=1e-13 * np.abs(want).max())
