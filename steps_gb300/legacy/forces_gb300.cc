@@ -22,12 +22,15 @@
  *
  * Precision: STEPS_GB300_PRECISION=fp64|mixed in the environment, default
  * mixed (FP32 pair arithmetic, FP64 accumulation, p99 error <= 1e-5).
+ * Each call prints the reference CUDA build's wall-clock line to stdout
+ * unless STEPS_GB300_QUIET=1.
  */
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
+#include <chrono>
 #include <vector>
 
 #include "steps_gb300.h"
@@ -132,7 +135,7 @@ bool sync_particles()
     return true;
 }
 
-bool upload_table(const REAL *tab, long long count, int (*setter)(int, int, const double *), int a, int b)
+[[maybe_unused]] bool upload_table(const REAL *tab, long long count, int (*setter)(int, int, const double *), int a, int b)
 {
     if (tab == S.table_ptr && count == S.table_size) return true;
     std::vector<double> t((size_t)count);
@@ -146,14 +149,32 @@ bool upload_table(const REAL *tab, long long count, int (*setter)(int, int, cons
     return true;
 }
 
-int set_t3(int ng, int, const double *t) { return steps_gpu_set_table_t3(ng, t); }
-int set_s1(int nrho, int nz, const double *t) { return steps_gpu_set_table_s1r2(nrho, nz, t); }
+[[maybe_unused]] int set_t3(int ng, int, const double *t) { return steps_gpu_set_table_t3(ng, t); }
+[[maybe_unused]] int set_s1(int nrho, int nz, const double *t) { return steps_gpu_set_table_s1r2(nrho, nz, t); }
+
+// The per-call timing line the reference's CUDA build prints to stdout
+// (StePS/src/forces_cuda.cu:1115, :1372 "Force calculation finished ...", :1702
+// "Z-periodic force calculation finished ..."), so logs read the same.
+// STEPS_GB300_QUIET=1 silences it.
+struct CallTimer {
+    const char *prefix;
+    std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+    explicit CallTimer(const char *pre) : prefix(pre) {}
+    ~CallTimer()
+    {
+        static const bool quiet = getenv("STEPS_GB300_QUIET") && strcmp(getenv("STEPS_GB300_QUIET"), "1") == 0;
+        if (quiet) return;
+        double s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        printf("%sorce calculation finished on MPI task %i. Force calculation wall-clock time = %fs.\n", prefix, rank,
+               s);
+    }
+};
 
 void run(const steps_params &p, REAL *x, REAL *F, int ID_min, int ID_max)
 {
     if (ID_max < ID_min) return;  // an empty range: the reference's loops do nothing (forces.cc:520-556)
     if (!ensure_context() || !sync_particles()) return;
-    int ni = ID_max - ID_min + 1;
+    [[maybe_unused]] const int ni = ID_max - ID_min + 1;  // the FP32 build's conversion
     const double *xd;
     double *Fd;
 #ifdef USE_SINGLE_PRECISION
@@ -223,6 +244,7 @@ void recalculate_softening()
 #if !defined(PERIODIC) && !defined(PERIODIC_Z)
 void forces(REAL *x, REAL *F, int ID_min, int ID_max)
 {
+    CallTimer timer("F");
     steps_params p = base_params(STEPS_R3);
     run(p, x, F, ID_min, ID_max);
 }
@@ -231,7 +253,9 @@ void forces(REAL *x, REAL *F, int ID_min, int ID_max)
 #ifdef PERIODIC
 void forces_periodic(REAL *x, REAL *F, int ID_min, int ID_max)
 {
+    CallTimer timer("F");
     steps_params p = base_params(STEPS_T3);
+    if (ID_max < ID_min) return;  // empty range: no work, no table upload
     if (IS_PERIODIC >= 2) {
         if (!ensure_context()) return;
         long long cnt = 3LL * N_EWALD_FORCE_GRID * N_EWALD_FORCE_GRID * N_EWALD_FORCE_GRID;
@@ -244,7 +268,9 @@ void forces_periodic(REAL *x, REAL *F, int ID_min, int ID_max)
 #ifdef PERIODIC_Z
 void forces_periodic_z(REAL *x, REAL *F, int ID_min, int ID_max)
 {
+    CallTimer timer("Z-periodic f");
     steps_params p = base_params(STEPS_S1R2);
+    if (ID_max < ID_min) return;  // empty range: no work, no table upload
     if (!ensure_context()) return;
 #ifdef PERIODIC_Z_NOLOOKUP
     p.s1r2_images = 1;
