@@ -86,3 +86,42 @@ def test_kdk_periodic_wrap(engine, port, topo):
             assert rel_err(Fg, Fo).max() < ftol
         else:
             assert err_stats(Fg, Fo)["p99"] < ftol
+
+
+def test_cfg0_force_and_four_kdk_steps(engine, port):
+    """The N = 32,768 compactified R^3 workload exactly as specified: plain
+    FP64, one force evaluation, then 4 KDK steps at fixed dt = 1e-3 from rest,
+    against the oracle's force + KDK on the same seeded input (one full
+    force evaluation and 4 steps, 5.4e9 pairs on the host). Mixed precision
+    on the same run meets the 1e-5 p99 bar on the final forces."""
+    import math
+
+    from steps_gb300 import workloads as W
+
+    ps = W.workload("cfg0")
+    n, dt = ps.m.size, 1e-3
+    assert n == 32768
+    rho_part = float(ps.m.min()) / (4.0 * math.pi * W.PARTICLE_RADII ** 3 / 3.0)
+    s = port.system(0, ps.m, ps.eps, port_params(O))
+    F0 = port.forces(s, ps.x)
+    xo, vo, Fo, eo = port.kdk(s, 4, dt, ps.x, np.zeros_like(ps.x), F0, rho_part=rho_part)
+    engine.set_particles(ps.m, ps.eps)
+    for precision in (S.FP64, S.MIXED):
+        engine.upload_positions(ps.x)
+        engine.upload_velocities(np.zeros_like(ps.x))
+        e = engine.kdk(S.params(S.R3), precision, 4, dt, rho_part=rho_part)
+        x, v, F = engine.state()
+        # displacements over the 4 steps (~1e-5 Mpc, far below the positions' ulp scale)
+        dg, do = x - ps.x, xo - ps.x
+        if precision == S.FP64:
+            # 1e-9 of the displacement, plus the rounding of x + v h (a few ulp of x)
+            ulp = np.spacing(np.maximum(np.abs(x), np.abs(xo)))
+            assert (np.abs(dg - do) <= 1e-9 * np.abs(do) + 4 * ulp).all()
+            assert rel_err(v, vo).max() < 1e-10
+            assert rel_err(F, Fo).max() < 1e-10
+            assert abs(e - eo) <= 1e-10 * abs(eo)
+        else:
+            assert err_stats(dg, do)["p99"] < 1e-5
+            assert np.abs(dg - do).max() <= 1e-3 * np.abs(do).max()
+            assert err_stats(F, Fo)["p99"] < 1e-5
+            assert abs(e - eo) <= 1e-4 * abs(eo)
