@@ -193,6 +193,11 @@ class Ref:
         self.lib.ref_softening(C.c_double(radius), _d(out))
         return out
 
+    def set_velocities(self, v):
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        assert v.shape == (self.n, 3)
+        self.lib.ref_set_velocities(_d(v))
+
     def set_params(self, is_periodic=0, L=0.0, rsim=0.0, cosmology=0, comoving=0, mius=0.0, h0=0.0, oml=0.0):
         self.lib.ref_set_params(C.c_int(is_periodic), C.c_double(L), C.c_double(rsim), C.c_int(cosmology),
                                 C.c_int(comoving), C.c_double(mius), C.c_double(h0), C.c_double(oml))

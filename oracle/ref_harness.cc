@@ -136,6 +136,12 @@ void ref_set_particles(int n, const double *xin, const double *m, const double *
     for (int i = 0; i < n; i++) { M[i] = (REAL)m[i]; SOFT_LENGTH[i] = (REAL)eps[i]; }
 }
 
+/* Overwrites the velocities v[3N] (set_particles starts them at zero). */
+void ref_set_velocities(const double *vin)
+{
+    for (int i = 0; i < 3 * N; i++) v[i] = (REAL)vin[i];
+}
+
 /* The reference's own softening law (utils.cc:59-82) with PARTICLE_RADII = radius.
  * Overwrites SOFT_LENGTH and returns it in eps_out; also sets M_min and rho_part. */
 void ref_softening(double radius, double *eps_out)

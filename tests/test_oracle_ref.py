@@ -85,3 +85,61 @@ def test_table_builders_other_sizes(port):
     want = O.Ref("s1o2").build_s1r2_table(40, 12, rmax, lz, 0.787875 / lz, 4, 10)
     got = port.s1r2_table(40, 12, rmax, lz, 0.787875 / lz, 4, 10)
     np.testing.assert_allclose(got, want, rtol=0, atol=1e-13 * np.abs(want).max())
+
+
+def _kdk_case(topo):
+    """(variant, particle set, reference params, port system factory, moving axes)
+    for a periodic KDK run; velocities move particles up to 2 % of L per step
+    so that many cross the boundary."""
+    if topo == "t3":
+        g = golden("t3_o2")
+        L, ng = float(g["L"]), int(g["ngrid"])
+        ps = W.t3_clumpy(1200, L, seed=305, n_clumps=6)
+        kw = dict(is_periodic=2, L=L, rsim=L / 2)
+        return ("t3o2", ps, kw, g["table"], ng, 3, L,
+                lambda port, eps: port.system(1, ps.m, eps, port_params(O, **kw), table=g["table"], ngrid=ng, order=2))
+    g = golden("s1r2_table_o2") if topo == "s1tab" else golden("s1r2_images")
+    L, rsim = float(g["L"]), float(g["rsim"])
+    ps = W.s1r2_cylindrical(1200, L, rsim, seed=306)
+    kw = dict(is_periodic=2, L=L, rsim=rsim)
+    if topo == "s1tab":
+        nrho, nz = (int(v) for v in g["shape"])
+        return ("s1o2", ps, kw, g["table"], (nrho, nz), 1, L,
+                lambda port, eps: port.system(2, ps.m, eps, port_params(O, **kw), table=g["table"], nrho=nrho, nz=nz,
+                                              order=2))
+    return ("s1nl", ps, kw, None, None, 1, L, lambda port, eps: port.system(3, ps.m, eps, port_params(O, **kw)))
+
+
+@pytest.mark.parametrize("topo", ["t3", "s1img", "s1tab"])
+def test_kdk_periodic_against_reference_step(port, topo):
+    """The oracle's KDK (the checker of the GPU KDK tests) against the
+    reference's own step() (StePS/src/step.cc:100-312) on a periodic
+    topology, with the boundary wrap exercised: positions, velocities,
+    forces and errmax after 3 fixed-dt steps."""
+    var, ps, kw, table, shape, axes, L, sysf = _kdk_case(topo)
+    ref = O.Ref(var)
+    ref.set_particles(ps.x, ps.m, ps.eps)
+    eps = ref.softening(W.PARTICLE_RADII)  # the reference's law; also sets rho_part for errmax
+    ref.set_params(**kw)
+    if var.startswith("t3"):
+        ref.set_t3_table(table, shape)
+    elif var == "s1o2":
+        ref.set_s1r2_table(table, *shape)
+    h, nsteps = 1e-3, 3
+    v = np.zeros_like(ps.x)
+    v[:, 3 - axes:] = np.random.default_rng(12).uniform(-1.0, 1.0, (ps.n, axes)) * (0.02 * L / h)
+    ref.set_velocities(v)
+    ref.forces_full()
+    for _ in range(nsteps):
+        ref.step(h)
+    xr, vr, Fr = ref.state()
+    er = ref.errmax()
+    s = sysf(port, eps)
+    rho_part = float(ps.m.min()) / (4.0 * math.pi * W.PARTICLE_RADII ** 3 / 3.0)
+    xo, vo, Fo, eo = port.kdk(s, nsteps, h, ps.x, v, port.forces(s, ps.x), rho_part=rho_part)
+    moved = np.abs(xr - ps.x)[:, 3 - axes:] > 0.5 * L
+    assert moved.any()  # some particles wrapped
+    np.testing.assert_allclose(xo, xr, rtol=0, atol=1e-12 * L)
+    assert rel_err(vo, vr).max() < 1e-12
+    assert rel_err(Fo, Fr).max() < 1e-11
+    assert abs(eo - er) <= 1e-12 * abs(er)
