@@ -60,3 +60,24 @@ def test_missing_library_fails_loudly(tmp_path):
             S.load_library(str(tmp_path / "libsteps_gb300.so"))
     finally:
         S._LIB = loaded
+
+
+def test_header_is_plain_c_and_links(tmp_path, lib):
+    """include/steps_gb300.h compiles as strict C99 and a C program that takes
+    the address of every declared entry point links against the library with
+    no unresolved symbol (the boundary needs no C++ on the caller's side)."""
+    import subprocess
+
+    names = declared_symbols()
+    src = tmp_path / "use_abi.c"
+    body = "\n".join(f"    (void (*)(void))&{n}," for n in names)
+    src.write_text('#include "steps_gb300.h"\n#include <stdio.h>\n'
+                   f"static void (*const entry_points[])(void) = {{\n{body}\n}};\n"
+                   "int main(void) { printf(\"%d\\n\", (int)(sizeof entry_points / sizeof *entry_points)); "
+                   "return 0; }\n")
+    exe = tmp_path / "use_abi"
+    lib_dir = os.path.join(ROOT, "steps_gb300", "_build")
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic", "-I",
+                        os.path.join(ROOT, "include"), str(src), "-o", str(exe), "-L", lib_dir, "-lsteps_gb300",
+                        "-Wl,--no-undefined"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
