@@ -122,7 +122,11 @@ int steps_gpu_get_table_t3(double *out);
 int steps_gpu_set_table_s1r2(int nrho, int nz, const double *table);
 
 /* Builds the S1xR2 table on the GPU (StePS/src/ewald_space.cc:618-798,
- * Tornberg 2015 singly periodic Ewald sums) for rho in [0, rho_max]. */
+ * Tornberg 2015 singly periodic Ewald sums) for rho in [0, rho_max].
+ * alpha = 0 with mmax = 0 -- the arguments of the reference's
+ * PERIODIC_Z_RSPACELOOKUP build (StePS/src/main.cc:650) -- builds it from
+ * direct real-space sums over nmax images per side instead, in that build's
+ * summation order (ewald_space.cc:710-750). */
 int steps_gpu_build_table_s1r2(int nrho, int nz, double rho_max, double lz, double alpha, int nmax, int mmax);
 int steps_gpu_get_table_s1r2(double *out);
 

@@ -160,7 +160,7 @@ class Port:
         return out
 
 
-REF_VARIANTS = ("r3", "t3o2", "t3o4", "s1nl", "s1o0", "s1o2", "s1o4", "r3sp", "t3o2sp", "s1nlsp")
+REF_VARIANTS = ("r3", "t3o2", "t3o4", "s1nl", "s1o0", "s1o2", "s1o4", "s1rs", "r3sp", "t3o2sp", "s1nlsp")
 
 
 def ref_available(variant: str = "r3") -> bool:

@@ -613,10 +613,47 @@ static double wrap_dz(double dz, double lz)
 /* Singly periodic (S1xR2) Ewald force per unit G m_i m_j, Tornberg (2015):
  * ewald_space.cc:618-752 (real-space images |n| <= nmax, modes m = 1..mmax,
  * and the m = 0 radial term). */
+/* Direct real-space image sum with no k-space part: the reference's
+ * PERIODIC_Z_RSPACELOOKUP build of S1R2ewald_force_pair (ewald_space.cc:710-750),
+ * n = 0 first, then -n and +n for n = 1..nmax (largest terms first). That
+ * build passes alpha = 0 and mmax = 0 (main.cc:650, :683), which select it here;
+ * the Ewald sums below reduce to the same terms at those arguments, in
+ * another order. */
+static void s1r2_pair_direct(double dx, double dy, double dz, double rho2, double lz, int nmax, double F[3])
+{
+    double Fx = 0, Fy = 0, Fz = 0;
+    double r2 = rho2 + dz * dz;
+    if (r2 >= 1e-18) {
+        double r = sqrt(r2);
+        double invr3 = 1.0 / (r2 * r);
+        Fx -= dx * invr3;
+        Fy -= dy * invr3;
+        Fz -= dz * invr3;
+    }
+    for (int n = 1; n <= nmax; ++n)
+        for (int sign = -1; sign <= 1; sign += 2) {
+            double dzn = dz + (double)(sign * n) * lz;
+            r2 = rho2 + dzn * dzn;
+            if (r2 < 1e-18) continue;
+            double r = sqrt(r2);
+            double invr3 = 1.0 / (r2 * r);
+            Fx -= dx * invr3;
+            Fy -= dy * invr3;
+            Fz -= dzn * invr3;
+        }
+    F[0] = Fx;
+    F[1] = Fy;
+    F[2] = Fz;
+}
+
 void oracle_s1r2_pair(double dx, double dy, double dz, double lz, double alpha, int nmax, int mmax, double F[3])
 {
     dz = wrap_dz(dz, lz);
     double rho2 = dx * dx + dy * dy;
+    if (alpha == 0.0 && mmax == 0) {
+        s1r2_pair_direct(dx, dy, dz, rho2, lz, nmax, F);
+        return;
+    }
     double rho = sqrt(rho2);
     double Fxr = 0, Fyr = 0, Fzr = 0;
     for (int n = -nmax; n <= nmax; ++n) {

@@ -205,7 +205,33 @@ __global__ void k_s1r2_table(int nrho, int nz, double rho_max, double lz, double
     double rho2 = dx * dx + dy * dy;
     double rr = sqrt(rho2);
     double Fxr = 0, Fzr = 0;
-    for (int n = -nmax; n <= nmax; ++n) {
+    // alpha = 0 with mmax = 0 is what the reference's PERIODIC_Z_RSPACELOOKUP
+    // build passes (StePS/src/main.cc:650, :683): a direct real-space image sum
+    // with no k-space part (StePS/src/ewald_space.cc:710-750), summed in its
+    // order -- n = 0, then -n, +n for n = 1..nmax -- for the same rounding.
+    const bool direct = alpha == 0.0 && mmax == 0;
+    if (direct) {
+        double r2 = rho2 + dz * dz;
+        if (r2 >= 1e-18) {
+            double r = sqrt(r2);
+            double invr3 = 1.0 / (r2 * r);
+            Fxr -= dx * invr3;
+            Fzr -= dz * invr3;
+        }
+    }
+    for (int n = direct ? 1 : -nmax; n <= nmax; ++n) {
+        if (direct) {
+            for (int sign = -1; sign <= 1; sign += 2) {
+                double dzn = dz + (double)(sign * n) * lz;
+                double r2 = rho2 + dzn * dzn;
+                if (r2 < 1e-18) continue;
+                double r = sqrt(r2);
+                double invr3 = 1.0 / (r2 * r);
+                Fxr -= dx * invr3;
+                Fzr -= dzn * invr3;
+            }
+            continue;
+        }
         double dzn = dz + (double)n * lz;
         double r2 = rho2 + dzn * dzn;
         if (r2 < 1e-18) continue;
@@ -306,8 +332,11 @@ int steps_gpu_build_table_s1r2(int nrho, int nz, double rho_max, double lz, doub
             Ctx &c = ctx();
             if (a.nrho < 1 || a.nz < 1 || (long long)a.nrho * a.nz > (1LL << 28))
                 fail(STEPS_E_ARG, "build_table_s1r2: bad shape");
-            if (!(a.lz > 0) || !(a.alpha > 0) || !(a.rho_max >= 0) || a.nmax < 0 || a.mmax < 0 || a.nmax > 10000 ||
-                a.mmax > 10000)
+            // alpha = 0 with mmax = 0: direct real-space sums, up to the 1e5 images
+            // per side of the reference's IS_PERIODIC >= 4 setting (StePS/src/main.cc:624).
+            const bool direct = a.alpha == 0.0 && a.mmax == 0;
+            if (!(a.lz > 0) || !(direct || a.alpha > 0) || !(a.rho_max >= 0) || a.nmax < 0 || a.mmax < 0 ||
+                a.nmax > (direct ? 100000 : 10000) || a.mmax > 10000)
                 fail(STEPS_E_ARG, "build_table_s1r2: bad Ewald parameters");
             size_t cnt = 2 * (size_t)a.nrho * a.nz;
             double *tab = c.s1r2.ensure<double>(cnt);

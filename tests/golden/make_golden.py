@@ -8,7 +8,8 @@ machine, and the GPU tests check the CUDA kernels against them.
 
 Run from the repository root:  python tests/golden/make_golden.py
 (``... make_golden.py fp32`` regenerates only the single-precision floor,
-``... make_golden.py background`` only the S1xR2 background-term vectors).
+``... make_golden.py background`` only the S1xR2 background-term vectors,
+``... make_golden.py rspace`` only the direct-sum S1xR2 table).
 """
 from __future__ import annotations
 
@@ -212,12 +213,28 @@ def fp32_floor():
          r3_F64=out["r3"], r3_F32=out["r3sp"], t3o2_F32=t3sp, s1r2_is2_F32=s1sp)
 
 
+def s1_rspace():
+    """The (rho, z) table of the reference's PERIODIC_Z_RSPACELOOKUP build:
+    direct real-space image sums, no k-space part (StePS/src/ewald_space.cc:
+    710-750), with the arguments that build passes (alpha = 0, mmax = 0,
+    StePS/src/main.cc:650) at a small grid and 1000 images per side (the
+    IS_PERIODIC = 2 setting, main.cc:608)."""
+    nz = 16
+    nrho = int(math.floor(nz * 2.25 * S1_RSIM / S1_LZ))
+    table = O.Ref("s1rs").build_s1r2_table(nrho, nz, 2.25 * S1_RSIM, S1_LZ, 0.0, 1000, 0)
+    save("s1r2_table_rspace", table=table, shape=np.array([nrho, nz]), L=np.array(S1_LZ), rsim=np.array(S1_RSIM),
+         nmax=np.array(1000))
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["fp32"]:
         fp32_floor()
     elif sys.argv[1:] == ["background"]:
         s1_background()
+    elif sys.argv[1:] == ["rspace"]:
+        s1_rspace()
     else:
         main()
         fp32_floor()
         s1_background()
+        s1_rspace()

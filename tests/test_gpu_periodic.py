@@ -142,6 +142,17 @@ def test_s1r2_table_builder(engine):
     np.testing.assert_allclose(tab, g["table"], rtol=0, atol=1e-12 * np.abs(g["table"]).max())
 
 
+def test_s1r2_table_builder_direct_sum(engine):
+    """alpha = 0 and mmax = 0 (what the reference's PERIODIC_Z_RSPACELOOKUP
+    build passes) build the table from direct real-space image sums in the
+    reference's order: IEEE-exact operations only, so equal to its table."""
+    g = golden("s1r2_table_rspace")
+    nrho, nz = (int(v) for v in g["shape"])
+    engine.build_table_s1r2(nrho, nz, 2.25 * float(g["rsim"]), float(g["L"]), 0.0, int(g["nmax"]), 0)
+    tab = engine.get_table_s1r2()
+    np.testing.assert_allclose(tab, g["table"], rtol=0, atol=1e-15 * np.abs(g["table"]).max())
+
+
 @pytest.mark.parametrize("order", [2, 4])
 def test_t3_fp64(engine, order):
     g = golden(f"t3_o{order}")

@@ -118,6 +118,17 @@ def test_s1r2_table(port, order):
     assert rel_err(port.forces(s, g["x"]), g["F"]).max() < TOL
 
 
+def test_s1r2_table_direct_sum(port):
+    """The (rho, z) table of the reference's PERIODIC_Z_RSPACELOOKUP build
+    (direct real-space image sums, selected by alpha = 0 and mmax = 0):
+    the same terms in the same order, so bit-identical."""
+    g = golden("s1r2_table_rspace")
+    nrho, nz = (int(v) for v in g["shape"])
+    L, rsim = float(g["L"]), float(g["rsim"])
+    tab = port.s1r2_table(nrho, nz, 2.25 * rsim, L, 0.0, int(g["nmax"]), 0)
+    assert np.array_equal(tab, g["table"])
+
+
 def test_s1r2_background_terms(port):
     """The S1xR2 background terms: comoving with the radial correction at
     IS_PERIODIC = 1, non-comoving H0^2 Omega_L x, and the table mode's plain

@@ -74,6 +74,15 @@ def test_s1r2_table(port, order):
     assert rel_err(port.forces(s, ps.x), ref.forces()).max() < TOL
 
 
+@pytest.mark.skipif(not O.ref_available("s1rs"), reason="reference build (oracle/_ref) not present")
+def test_s1r2_direct_sum_table_other_size(port):
+    """The direct real-space table (PERIODIC_Z_RSPACELOOKUP build) at another
+    grid, period and image count: bit-identical."""
+    lz, rmax = 90.0, 2.25 * 250.0
+    want = O.Ref("s1rs").build_s1r2_table(25, 10, rmax, lz, 0.0, 3000, 0)
+    assert np.array_equal(port.s1r2_table(25, 10, rmax, lz, 0.0, 3000, 0), want)
+
+
 def test_table_builders_other_sizes(port):
     """Both Ewald table builders at grid sizes the golden set does not use."""
     L = 80.0
