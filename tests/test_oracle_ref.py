@@ -152,3 +152,25 @@ def test_kdk_periodic_against_reference_step(port, topo):
     assert rel_err(vo, vr).max() < 1e-12
     assert rel_err(Fo, Fr).max() < 1e-11
     assert abs(eo - er) <= 1e-12 * abs(er)
+
+
+@pytest.mark.parametrize("order", [0, 2, 4])
+def test_s1r2_table_beyond_radial_extent(port, order):
+    """Pairs whose rho separation passes the table's radial extent
+    (2.25 Rsim): the reference clamps rho to the last table row; the
+    oracle must do the same."""
+    g = golden(f"s1r2_table_o{order}")
+    nrho, nz = (int(v) for v in g["shape"])
+    L, rsim = float(g["L"]), float(g["rsim"])
+    ps = W.s1r2_cylindrical(800, L, rsim, seed=307)
+    x = ps.x.copy()
+    x[:200, :2] *= 2.0  # out to 2 Rsim from the axis: separations up to 3 Rsim
+    rho = np.hypot(x[:, 0], x[:, 1])
+    assert rho.max() + np.hypot(ps.x[:, 0], ps.x[:, 1]).max() > 2.25 * rsim
+    ref = O.Ref(f"s1o{order}")
+    ref.set_particles(x, ps.m, ps.eps)
+    ref.set_params(is_periodic=2, L=L, rsim=rsim)
+    ref.set_s1r2_table(g["table"], nrho, nz)
+    s = port.system(2, ps.m, ps.eps, port_params(O, is_periodic=2, L=L, rsim=rsim), table=g["table"], nrho=nrho,
+                    nz=nz, order=order)
+    assert rel_err(port.forces(s, x), ref.forces()).max() < TOL
