@@ -25,7 +25,9 @@
  *     global x (StePS/src/global_variables.h:107);
  *   - forces are accelerations with G = 1, OVERWRITTEN (not accumulated) for
  *     i in [id_min, id_max] and stored at F[3*(i-id_min)+k], as
- *     forces.cc:520-526 and forces_cuda.cu:1045,1078-1097 return them;
+ *     forces.cc:520-526 and forces_cuda.cu:1045,1078-1097 return them: the
+ *     reference's CPU loop adds into F with += (forces.cc:550-556) but zeroes
+ *     F first, so values a caller pre-loads into F are lost there too;
  *   - one GPU, one internal CUDA stream; calls are synchronous from the
  *     caller's view (unless documented otherwise) and not re-entrant.
  */
@@ -224,8 +226,10 @@ int steps_gpu_set_precision_guard(double ratio);
 
 /* Times every supported mixed-precision shape on the resident particles for
  * the given topology -- for R^3 with each pair-loop variant -- and keeps the
- * fastest; writes threads, ipt, variant to out[3]. One evaluation per
- * candidate. */
+ * fastest; writes threads, ipt, variant to out[3]. Each candidate runs the
+ * pair kernel on a strided sample of the range's i tiles (about 8192 i
+ * particles against all j, at least two waves of work): one untimed launch,
+ * then the median of three timed ones. Leaves no resident forces. */
 int steps_gpu_autotune(const steps_params *p, int id_min, int id_max, int *out);
 
 /* Number of kernels this library has launched since init. */
@@ -280,13 +284,16 @@ int steps_gpu_test_stall_copy(long long tile_seq);
  * in device memory of the current device: x[3n] (AoS), m[n], eps[n] and
  * F[3*(id_max-id_min+1)] (overwritten). Calls no cudaMalloc, cudaFree or
  * allocating library routine and needs no steps_gpu_init. Asynchronous on
- * `stream` (a cudaStream_t; NULL = legacy default stream).
+ * `stream` (a cudaStream_t; NULL = legacy default stream). id_max = id_min - 1
+ * is the empty range: STEPS_OK with nothing computed (F may then be NULL).
  * Working memory is one static 32 MiB device array per GPU that loads the
  * library, held until exit: the i range is limited to 1,398,101 particles
  * (larger ranges return STEPS_E_ARG). The array's device address is looked
- * up by the first call on each device -- make that call before any stream
- * capture. All calls share the array (it keeps the last call's contents):
- * calls that overlap on the GPU race, so the caller serialises them. */
+ * up by the first call on each device, and again by the first call after a
+ * cudaDeviceReset -- make those calls before any stream capture. All calls
+ * share the array (it keeps the last call's contents; each call writes what
+ * it reads): calls that overlap on the GPU race, so the caller serialises
+ * them. */
 int steps_gpu_forces_fp64_noalloc(const steps_params *p, const double *x, const double *m, const double *eps, int n,
                                   double *F, int id_min, int id_max, void *stream);
 

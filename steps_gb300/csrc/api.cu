@@ -9,6 +9,8 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
+#include <atomic>
 #include <mutex>
 #include <string>
 
@@ -20,6 +22,9 @@ namespace steps {
 
 static Ctx g_ctx;
 static thread_local std::string g_err;
+// Kernels launched since steps_gpu_init. Atomic: the allocation-free entry
+// point needs no context and may be called from several host threads.
+static std::atomic<long long> g_launches{0};
 
 Ctx &ctx() { return g_ctx; }
 
@@ -33,9 +38,11 @@ void check_cuda(cudaError_t e, const char *what, const char *file, int line)
     fail(e == cudaErrorMemoryAllocation ? STEPS_E_NOMEM : STEPS_E_CUDA, buf);
 }
 
+void add_launches(long long k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
+
 void note_launch(const char *name)
 {
-    g_ctx.launches++;
+    g_launches.fetch_add(1, std::memory_order_relaxed);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         char buf[256];
@@ -214,7 +221,7 @@ int steps_gpu_init(int device)
         for (auto &e : c.marks) STEPS_CUDA(cudaEventCreate(&e));
         for (auto &e : c.phase) STEPS_CUDA(cudaEventCreate(&e));
         c.device = device;
-        c.launches = 0;
+        g_launches.store(0);
     });
 }
 
@@ -234,7 +241,7 @@ int steps_gpu_shutdown(void)
         TileSet *ts[] = {&c.tj, &c.ti};
         for (TileSet *t : ts) {
             for (int k = 0; k < 2; k++) { t->keys[k].release(); t->vals[k].release(); }
-            t->hist.release(); t->pack.release(); t->eps.release(); t->meta.release(); t->idx.release(); t->resid.release(); t->soa.release();
+            t->hist.release(); t->pack.release(); t->eps.release(); t->meta.release(); t->idx.release(); t->resid.release(); t->soa.release(); t->sub.release();
             *t = TileSet();
         }
         for (auto &e : c.marks) cudaEventDestroy(e);
@@ -456,6 +463,19 @@ int steps_gpu_autotune(const steps_params *p, int id_min, int id_max, int *out)
         KParams kp = derive_params(p);
         // R^3: the scalar and packed pair loops as well.
         const int nvar = kp.topology == STEPS_R3 ? R3_VARIANTS : 1;
+        // Each candidate runs the pair kernel on a strided sample of the real
+        // i tiles (about 8192 i particles, at least two waves of items; no
+        // reduction): one untimed launch, then the median of three timed ones.
+        struct SampleMode {
+            Ctx &c;
+            explicit SampleMode(Ctx &cc) : c(cc) { c.tune_sample = true; }
+            ~SampleMode()
+            {
+                c.tune_sample = false;
+                c.F_ni = 0;  // the sampled runs leave no usable forces
+                c.F_valid = false;
+            }
+        } mode(c);
         compute_forces(p, STEPS_MIXED, id_min, id_max, false);  // orders the particles, loads modules
         for (int v = 0; v < nvar; v++)
             for (auto &s : shapes) {
@@ -466,11 +486,15 @@ int steps_gpu_autotune(const steps_params *p, int id_min, int id_max, int *out)
                 c.shape.ipt = s[1];
                 c.shape.jsplit = 0;
                 c.shape.variant = v;
-                // one timed evaluation per candidate: the phase events bracket the pair kernel only
-                compute_forces(p, STEPS_MIXED, id_min, id_max, true);
-                STEPS_CUDA(cudaEventSynchronize(c.phase[2]));
-                float ms = 0;
-                STEPS_CUDA(cudaEventElapsedTime(&ms, c.phase[1], c.phase[2]));
+                float t[4];
+                for (int r = 0; r < 4; r++) {
+                    // the phase events bracket the pair kernel only
+                    compute_forces(p, STEPS_MIXED, id_min, id_max, true);
+                    STEPS_CUDA(cudaEventSynchronize(c.phase[2]));
+                    STEPS_CUDA(cudaEventElapsedTime(&t[r], c.phase[1], c.phase[2]));
+                }
+                std::sort(t + 1, t + 4);
+                const float ms = t[2];
                 if (ms < best) { best = ms; bestS = c.shape; }
             }
         c.shape = bestS;
@@ -506,7 +530,7 @@ int steps_gpu_set_kernel_variant(int variant)
     });
 }
 
-long long steps_gpu_launch_count(void) { return g_ctx.launches; }
+long long steps_gpu_launch_count(void) { return g_launches.load(); }
 
 double steps_gpu_last_phase_ms(int phase)
 {
@@ -546,7 +570,7 @@ int steps_gpu_flush_l2(long long bytes)
         require_init();
         if (bytes <= 0 || bytes > (8LL << 30)) fail(STEPS_E_ARG, "flush size out of range");
         void *p = g_ctx.flush.ensure<char>((size_t)bytes);
-        STEPS_CUDA(cudaMemsetAsync(p, (int)(g_ctx.launches & 0xff), (size_t)bytes, g_ctx.stream));
+        STEPS_CUDA(cudaMemsetAsync(p, (int)(g_launches.load() & 0xff), (size_t)bytes, g_ctx.stream));
     });
 }
 

@@ -157,6 +157,7 @@ void plan(Batch &b, int threads, int ipt)
     b.ts.idx.ensure<uint32_t>(padded);
     b.ts.resid.ensure<float4>(padded);
     b.ts.soa.ensure<float4>(padded);
+    b.ts.sub.ensure<float4>(2 * (padded / SUBTILE));
     b.part.ensure<double>((size_t)b.nitems * T * 3);
     b.T = T;
     b.threads = threads;
@@ -189,16 +190,19 @@ void batch_forces(Batch &b)
     sort_pairs(b.ts, b.ntot, st, std::max(0, 51 - std::min(51, morton_sort_bits(b.nmax))));
     tile_build_range(b.x.as<double>(), b.m64.as<double>(), b.eps64.as<double>(), b.ts.perm(), b.ntot, b.T,
                      b.ts.pack.as<float4>(), b.ts.eps.as<float>(), b.ts.meta.as<float4>(), b.ts.idx.as<uint32_t>(),
-                     PAD_J, b.ts.resid.as<float4>(), b.ts.soa.as<float>(), b.tdesc.as<int2>(), b.ntiles, st);
+                     PAD_J, b.ts.resid.as<float4>(), b.ts.soa.as<float>(), b.tdesc.as<int2>(), b.ntiles, st,
+                     b.ts.sub.as<float4>());
 
     mixed::MixedArgs a{};
     a.stall_seq = -1;
+    a.istride = 1;
     a.jpack = a.ipack = b.ts.pack.as<float4>();
     a.jeps = a.ieps = b.ts.eps.as<float>();
     a.jmeta = a.imeta = b.ts.meta.as<float4>();
     a.jidx = a.iidx = b.ts.idx.as<uint32_t>();
     a.jres = a.ilo = b.ts.resid.as<float4>();
     a.jsoa = b.ts.soa.as<float>();
+    a.jsub = b.ts.sub.as<float4>();
     a.njt = a.nit = b.ntiles;
     a.nitems = b.nitems;
     a.items = b.items.as<int4>();
@@ -286,7 +290,8 @@ void batch_release()
     release_graph(*b);
     DevBuf *bufs[] = {&b->x, &b->v, &b->F, &b->m64, &b->eps64, &b->rel, &b->bbox, &b->tdesc, &b->items, &b->tslot,
                       &b->part, &b->counter, &b->err, &b->ts.keys[0], &b->ts.keys[1], &b->ts.vals[0], &b->ts.vals[1],
-                      &b->ts.hist, &b->ts.pack, &b->ts.eps, &b->ts.meta, &b->ts.idx, &b->ts.resid, &b->ts.soa};
+                      &b->ts.hist, &b->ts.pack, &b->ts.eps, &b->ts.meta, &b->ts.idx, &b->ts.resid, &b->ts.soa,
+                      &b->ts.sub};
     for (DevBuf *d : bufs) d->release();
     delete b;
     c.batch = nullptr;
@@ -438,7 +443,7 @@ int steps_gpu_batch_run(const steps_params *p, int precision, int nsteps, double
                 b.graph_h = a.h;
             }
             STEPS_CUDA(cudaGraphLaunch(b.exec, c.stream));
-            c.launches += b.graph_kernels;  // the kernels the graph runs
+            add_launches(b.graph_kernels);  // the kernels the graph runs
             STEPS_CUDA(cudaStreamSynchronize(c.stream));
         },
         &args);

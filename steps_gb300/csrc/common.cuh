@@ -75,6 +75,7 @@ struct TileSet {
     DevBuf idx;  // idx[q] = original index of curve position q; padding holds pad_id
     DevBuf resid;  // resid[q] = (x - c) - pack[q].xyz, the FP32 residual of the offset
     DevBuf soa;    // tile-blocked SoA copy of pack: X[T], Y[T], Z[T], M[T] per tile
+    DevBuf sub;    // per SUBTILE particles: (box centre offset, eps_max), (half extents, 0)
     int perm_sel = 0;  // vals[perm_sel] holds curve position -> original index
     bool ordered = false;
     const uint32_t *perm() const { return vals[perm_sel].as<uint32_t>(); }
@@ -95,8 +96,14 @@ struct Shape {
 
 inline __host__ __device__ int div_up(int a, int b) { return (a + b - 1) / b; }
 
+// Particles per j sub-tile: the near/far decision of the packed R^3 kernel is
+// taken per (warp, sub-tile) from the sub-tile boxes the tile build writes.
+constexpr int SUBTILE = 16;
+
 // Kernel-launch bookkeeping: counts launches and surfaces launch errors.
 void note_launch(const char *name);
+// Adds kernels launched by other means (the kernel nodes of a graph launch).
+void add_launches(long long k);
 
 // ---------------------------------------------------- device math helpers --
 

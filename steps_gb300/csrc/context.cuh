@@ -16,7 +16,6 @@ struct Ctx {
     bool mark_set[16] = {};
     cudaEvent_t phase[4] = {};
     bool phase_valid = false;
-    long long launches = 0;
 
     int n = 0;                       // particle count fixed by set_particles
     DevBuf m64, eps64;               // masses, softening (FP64, original order)
@@ -52,6 +51,7 @@ struct Ctx {
 
     Shape shape;
     bool shape_fixed = false;
+    bool tune_sample = false;  // the autotuner's timing runs: a strided sample of i tiles, no reduction
     double last_pairs = 0.0;
 
     Batch *batch = nullptr;
@@ -77,7 +77,7 @@ void batch_keys(const double *x, int lo, int count, unsigned long long prefix, u
                 unsigned long long *bbox_scratch, cudaStream_t st);
 void tile_build_range(const double *x, const double *m64, const double *eps64, const uint32_t *perm, int count, int T,
                       float4 *pack, float *epsf, float4 *meta, uint32_t *idx, uint32_t pad_id, float4 *lo, float *soa,
-                      const int2 *tdesc, int ntiles, cudaStream_t st);
+                      const int2 *tdesc, int ntiles, cudaStream_t st, float4 *sub);
 
 // pair_fp64.cu: FP64 forces of i in [id_min, id_min+ni) into F[3*ni] (with background).
 void forces_fp64(const KParams &kp, const Tables &tb, const double *x, int n, int id_min, int ni, double *F);

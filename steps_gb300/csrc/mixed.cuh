@@ -16,6 +16,7 @@ struct MixedArgs {
     const uint32_t *jidx;
     const float4 *jres;  // FP32 residuals of the j offsets (double-float near path)
     const float *jsoa;   // tile-blocked SoA copy of jpack (packed-FP32 kernel)
+    const float4 *jsub;  // j sub-tile boxes, 2 float4 per SUBTILE particles (packed-FP32 kernel)
     int njt;
     const float4 *ipack;
     const float *ieps;
@@ -25,6 +26,7 @@ struct MixedArgs {
     int nit;
     int S, tpc;  // j chunks per i tile, j tiles per chunk
     int nitems;
+    int istride;  // item -> i tile (item / S) * istride: 1, or > 1 when the autotuner times a sample of i tiles
     unsigned *counter;
     int *status;        // STEPS_E_TIMEOUT written here by a pipeline wait that gave up
     long long stall_seq;  // test hook: block 0 withholds the copy of its tile number stall_seq (-1: none)
@@ -206,6 +208,26 @@ __device__ __forceinline__ bool warp_full(float dOx, float dOy, float dOz, float
     const float gx = axis_gap(dx, hw.x, hJ.x), gy = axis_gap(dy, hw.y, hJ.y), gz = axis_gap(dz, hw.z, hJ.z);
     const float g2 = gx * gx + gy * gy + gz * gz;
     return g2 <= bmax * bmax * 1.0001f + 1e-30f || coarse_for_gap(dx, dy, dz, hw, hJ, g2, guard2);
+}
+
+// warp_full for one j sub-tile: box centre s (offset from J's centre, with
+// the sub-tile's largest softening in s.w) and half extents hs. The gap is the
+// sub-tile's; the FP32 error scale stays that of the offsets actually used --
+// i in J's frame (|d_O - c| + |h|) and j relative to J's centre (|s| + |hs|).
+__device__ __forceinline__ bool warp_full_sub(float dOx, float dOy, float dOz, float4 s, float4 hs, float4 c,
+                                              float4 h, float wemax, float guard2)
+{
+    const float ex = dOx - c.x, ey = dOy - c.y, ez = dOz - c.z;  // J's centre from the warp box centre
+    const float dx = ex + s.x, dy = ey + s.y, dz = ez + s.z;
+    const float4 hw = make_float4(h.x + 1e-6f * (fabsf(ex) + fabsf(s.x) + fabsf(c.x)),
+                                  h.y + 1e-6f * (fabsf(ey) + fabsf(s.y) + fabsf(c.y)),
+                                  h.z + 1e-6f * (fabsf(ez) + fabsf(s.z) + fabsf(c.z)), 0.0f);
+    const float gx = axis_gap(dx, hw.x, hs.x), gy = axis_gap(dy, hw.y, hs.y), gz = axis_gap(dz, hw.z, hs.z);
+    const float g2 = gx * gx + gy * gy + gz * gz;
+    const float bmax = wemax + s.w;
+    const float sc = sqrtf(ex * ex + ey * ey + ez * ez) + sqrtf(hw.x * hw.x + hw.y * hw.y + hw.z * hw.z) +
+                     sqrtf(s.x * s.x + s.y * s.y + s.z * s.z) + sqrtf(hs.x * hs.x + hs.y * hs.y + hs.z * hs.z);
+    return g2 <= bmax * bmax * 1.0001f + 1e-30f || sc * sc > guard2 * g2;
 }
 
 // Packed FP32 pairs (PTX .f32x2, sm_100+).

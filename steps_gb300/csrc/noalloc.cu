@@ -22,7 +22,16 @@
 //
 // The device address of the array is looked up once per device with
 // cudaGetSymbolAddress, by the first call made while that device is current;
-// make that first call before any stream capture.
+// make that first call before any stream capture. The address is kept
+// together with the CUDA context it was found in: after a cudaDeviceReset
+// (which unloads the library's device code with the context) the next call
+// finds a new context and looks the address up again, so that call too
+// belongs before any stream capture.
+//
+// The empty i range id_max = id_min - 1 is accepted and does nothing (F may
+// then be NULL), as in every other force entry point.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "common.cuh"
@@ -41,6 +50,40 @@ constexpr int NA_MAX_DEVICES = 64;
 
 std::mutex g_na_mutex;
 double *g_na_ptr[NA_MAX_DEVICES] = {};
+CUcontext g_na_ctx[NA_MAX_DEVICES] = {};  // the context each cached address belongs to
+
+// cuCtxGetCurrent through the runtime's driver entry-point query (no link
+// dependency on libcuda). Called with g_na_mutex held.
+CUcontext current_context()
+{
+    using Fn = CUresult (*)(CUcontext *);
+    static Fn fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !p) {
+            cudaGetLastError();
+            fail(STEPS_E_CUDA, "noalloc: cuCtxGetCurrent is not available from the driver");
+        }
+        fn = reinterpret_cast<Fn>(p);
+    }
+    CUcontext c = nullptr;
+    if (fn(&c) != CUDA_SUCCESS) fail(STEPS_E_CUDA, "noalloc: cuCtxGetCurrent failed");
+    return c;  // NULL while this thread has made no CUDA runtime call yet
+}
+
+double *lookup_scratch()
+{
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+        cudaGetLastError();
+        fail(STEPS_E_CUDA,
+             std::string("cudaGetSymbolAddress of the no-allocation scratch failed: ") + cudaGetErrorString(e));
+    }
+    return static_cast<double *>(p);
+}
 
 // Host-side address of the scratch array on the current device. In host code
 // the symbol itself is only a stand-in, never a device address.
@@ -50,17 +93,15 @@ double *scratch_on_current_device()
     STEPS_CUDA(cudaGetDevice(&dev));
     if (dev < 0 || dev >= NA_MAX_DEVICES) fail(STEPS_E_ARG, "device index out of range for the no-allocation path");
     std::lock_guard<std::mutex> lock(g_na_mutex);
-    if (!g_na_ptr[dev]) {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) {
-            cudaGetLastError();
-            fail(STEPS_E_CUDA, std::string("cudaGetSymbolAddress of the no-allocation scratch failed: ") +
-                                   cudaGetErrorString(e));
-        }
-        g_na_ptr[dev] = static_cast<double *>(p);
-    }
-    return g_na_ptr[dev];
+    CUcontext cur = current_context();
+    if (cur && g_na_ptr[dev] && g_na_ctx[dev] == cur) return g_na_ptr[dev];
+    // First call on this device, or a new context: the lookup also binds the
+    // device's primary context to this thread when none is current yet.
+    double *p = lookup_scratch();
+    if (!cur) cur = current_context();
+    g_na_ptr[dev] = p;
+    g_na_ctx[dev] = cur;
+    return p;
 }
 
 // Same pair arithmetic as the plain FP64 R^3 kernel (ascending j per i,
@@ -139,11 +180,15 @@ extern "C" int steps_gpu_forces_fp64_noalloc(const steps_params *p, const double
     return run_guarded(
         [](void *vp) {
             A &a = *static_cast<A *>(vp);
-            if (!a.p || !a.x || !a.m || !a.eps || !a.F) fail(STEPS_E_ARG, "noalloc: every pointer must be non-NULL");
+            if (!a.p) fail(STEPS_E_ARG, "noalloc: params is NULL");
             if (a.p->topology != STEPS_R3) fail(STEPS_E_ARG, "noalloc: only the R^3 topology is available");
-            if (a.n <= 0 || a.id_min < 0 || a.id_max >= a.n || a.id_max < a.id_min)
+            // id_max = id_min - 1 is the empty range (StePS/src/forces.cc:520-556
+            // loops over nothing): no work, F may be NULL.
+            if (a.n <= 0 || a.id_min < 0 || a.id_min > a.n || a.id_max >= a.n || a.id_max < a.id_min - 1)
                 fail(STEPS_E_ARG, "noalloc: i range outside [0, n)");
             const int ni = a.id_max - a.id_min + 1;
+            if (ni == 0) return;
+            if (!a.x || !a.m || !a.eps || !a.F) fail(STEPS_E_ARG, "noalloc: every pointer must be non-NULL");
             const size_t cap = STEPS_NOALLOC_SCRATCH_BYTES / (3 * sizeof(double));  // i-rows of partial forces
             if ((size_t)ni > cap)
                 fail(STEPS_E_ARG, "noalloc: i range of " + std::to_string(ni) + " particles exceeds the " +

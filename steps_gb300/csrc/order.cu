@@ -173,7 +173,8 @@ __global__ void __launch_bounds__(TB_THREADS) k_tile_build(const double *__restr
                                                           float4 *__restrict__ pack, float *__restrict__ epsf,
                                                           float4 *__restrict__ meta, uint32_t *__restrict__ idx,
                                                           uint32_t pad_id, float4 *__restrict__ lo,
-                                                          float *__restrict__ soa, const int2 *__restrict__ tdesc)
+                                                          float *__restrict__ soa, const int2 *__restrict__ tdesc,
+                                                          float4 *__restrict__ sub)
 {
     __shared__ double red[7][TB_THREADS / 32];
     __shared__ float s_c[3];
@@ -256,6 +257,35 @@ __global__ void __launch_bounds__(TB_THREADS) k_tile_build(const double *__restr
             epsf[q] = 0.f;
             if (idx) idx[q] = pad_id;
         }
+        if (sub) {
+            // Sub-tile boxes: the SUBTILE consecutive particles of a half warp
+            // (padding included, at the tile centre), in the tile's FP32 offset
+            // frame, widened by 1e-6 relative so they hold the exact positions.
+            const float4 pq = pack[q];
+            float l3[3] = {pq.x, pq.y, pq.z}, h3[3] = {pq.x, pq.y, pq.z};
+            float se = epsf[q];
+#pragma unroll
+            for (int o = SUBTILE / 2; o > 0; o >>= 1) {
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    l3[k] = fminf(l3[k], __shfl_xor_sync(0xffffffffu, l3[k], o));
+                    h3[k] = fmaxf(h3[k], __shfl_xor_sync(0xffffffffu, h3[k], o));
+                }
+                se = fmaxf(se, __shfl_xor_sync(0xffffffffu, se, o));
+            }
+            if ((e & (SUBTILE - 1)) == 0) {
+                float c3[3], w3[3];
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    c3[k] = 0.5f * (l3[k] + h3[k]);
+                    const float w = fmaxf(h3[k] - c3[k], c3[k] - l3[k]);
+                    w3[k] = w * 1.000001f + 1e-6f * (fabsf(c3[k]) + w) + 1e-30f;
+                }
+                float4 *d = sub + 2 * ((size_t)tile * (T / SUBTILE) + e / SUBTILE);
+                d[0] = make_float4(c3[0], c3[1], c3[2], se);
+                d[1] = make_float4(w3[0], w3[1], w3[2], 0.0f);
+            }
+        }
     }
 }
 
@@ -326,9 +356,11 @@ void build_tiles(TileSet &ts, const double *x, const double *m64, const double *
     ts.idx.ensure<uint32_t>(padded);
     ts.resid.ensure<float4>(padded);
     ts.soa.ensure<float4>(padded);
+    ts.sub.ensure<float4>(2 * (padded / SUBTILE));
     k_tile_build<<<ts.ntiles, TB_THREADS, 0, st>>>(x, m64, eps64, ts.perm(), count, T, ts.pack.as<float4>(),
                                                    ts.eps.as<float>(), ts.meta.as<float4>(), ts.idx.as<uint32_t>(),
-                                                   pad_id, ts.resid.as<float4>(), ts.soa.as<float>(), nullptr);
+                                                   pad_id, ts.resid.as<float4>(), ts.soa.as<float>(), nullptr,
+                                                   ts.sub.as<float4>());
     note_launch("k_tile_build");
 }
 
@@ -348,11 +380,11 @@ void batch_keys(const double *x, int lo, int count, unsigned long long prefix, u
 
 void tile_build_range(const double *x, const double *m64, const double *eps64, const uint32_t *perm, int count, int T,
                       float4 *pack, float *epsf, float4 *meta, uint32_t *idx, uint32_t pad_id, float4 *lo, float *soa,
-                      const int2 *tdesc, int ntiles, cudaStream_t st)
+                      const int2 *tdesc, int ntiles, cudaStream_t st, float4 *sub)
 {
     int nt = tdesc ? ntiles : div_up(count, T);
     k_tile_build<<<nt, TB_THREADS, 0, st>>>(x, m64, eps64, perm, count, T, pack, epsf, meta, idx, pad_id, lo, soa,
-                                            tdesc);
+                                            tdesc, sub);
     note_launch("k_tile_build");
 }
 

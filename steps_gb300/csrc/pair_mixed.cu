@@ -52,8 +52,8 @@ __global__ void __launch_bounds__(BLOCK, KIND == K_R3 && IPT == 1 ? 1024 / BLOCK
         __syncthreads();
         const int item = s_item;
         if (item >= a.nitems) return;
-        const int I = item / a.S;
-        const int chunk = item - I * a.S;
+        const int I = (item / a.S) * a.istride;
+        const int chunk = item % a.S;
         const int J0 = chunk * a.tpc;
         const int J1 = min(a.njt, J0 + a.tpc);
 
@@ -512,6 +512,7 @@ void forces_mixed(const KParams &kp, const Tables &tb, const double *x, const do
     a.jidx = c.tj.idx.as<uint32_t>();
     a.jres = c.tj.resid.as<float4>();
     a.jsoa = c.tj.soa.as<float>();
+    a.jsub = c.tj.sub.as<float4>();
     a.njt = njt;
     a.ipack = ti.pack.as<float4>();
     a.ieps = ti.eps.as<float>();
@@ -522,6 +523,17 @@ void forces_mixed(const KParams &kp, const Tables &tb, const double *x, const do
     a.S = S;
     a.tpc = tpc;
     a.nitems = nit * S;
+    a.istride = 1;
+    // The autotuner times a strided sample of the real i tiles (dense tiles,
+    // the same j split): at least 8192 i particles and two waves of items.
+    const bool sample = c.tune_sample;
+    if (sample) {
+        const int want = std::max(div_up(8192, T), div_up(2 * resident, S));
+        if (want < nit) {
+            a.istride = nit / want;
+            a.nitems = want * S;
+        }
+    }
     a.counter = c.counter.ensure<unsigned>(4);
     a.items = nullptr;
     a.part_stride = (size_t)nit * T * 3;
@@ -566,12 +578,15 @@ void forces_mixed(const KParams &kp, const Tables &tb, const double *x, const do
         if (*c.kstatus_host != 0) fail(STEPS_E_TIMEOUT, "pair kernel: a pipeline wait timed out (status written by the kernel)");
     }
     STEPS_CUDA(cudaEventRecord(c.phase[2], st));
-    k_reduce_mixed<<<div_up(ni, 256), 256, 0, st>>>(a.part, S, a.part_stride, ti.perm(), ni, id_min, x,
-                                                   background_of(kp, tb), F);
-    note_launch("k_reduce_mixed");
+    if (!sample) {
+        k_reduce_mixed<<<div_up(ni, 256), 256, 0, st>>>(a.part, S, a.part_stride, ti.perm(), ni, id_min, x,
+                                                       background_of(kp, tb), F);
+        note_launch("k_reduce_mixed");
+    }
     STEPS_CUDA(cudaEventRecord(c.phase[3], st));
     c.phase_valid = true;
-    c.last_pairs = (double)ni * (double)n;
+    c.last_pairs = (double)(a.nitems / S) * T * (double)n;
+    if (!sample) c.last_pairs = (double)ni * (double)n;
 }
 
 }  // namespace steps

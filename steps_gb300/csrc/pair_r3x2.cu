@@ -23,11 +23,14 @@ namespace {
 using namespace mixed;
 
 template <int BLOCK, int IPT>
-__device__ __forceinline__ void stage_soa(const MixedArgs &a, int J, float *sx, float *se, uint32_t *sid, float4 *sres)
+__device__ __forceinline__ void stage_soa(const MixedArgs &a, int J, float *sx, float *se, uint32_t *sid, float4 *sres,
+                                          float4 *ssub)
 {
     constexpr int T = BLOCK * IPT;
+    constexpr int NS2 = 2 * (T / SUBTILE);  // float4 of sub-tile boxes per tile
     const float4 *src = reinterpret_cast<const float4 *>(a.jsoa + (size_t)J * 4 * T);
     float4 *dst = reinterpret_cast<float4 *>(sx);
+    for (int e = threadIdx.x; e < NS2; e += BLOCK) cp_async16(ssub + e, a.jsub + (size_t)J * NS2 + e);
 #pragma unroll
     for (int k = 0; k < IPT; k++) {  // 4T floats = T float4 chunks
         const int e = k * BLOCK + threadIdx.x;
@@ -40,112 +43,157 @@ __device__ __forceinline__ void stage_soa(const MixedArgs &a, int J, float *sx, 
     cp_commit();
 }
 
+// v, made to depend on dep (an opaque move): keeps a computation from v
+// inside the loop that dep varies in.
+__device__ __forceinline__ float pin_to(float v, int dep)
+{
+    float r;
+    asm("mov.b32 %0, %1; // %2" : "=f"(r) : "f"(v), "r"(dep));
+    return r;
+}
+
 // One j tile J against this thread's i particles: the staged tile is sxb
 // (X[T], Y[T], Z[T], M[T]), seb (softening), sidb (ids), sresb (residuals).
+// The near/far decision is taken per (warp, j sub-tile of SUBTILE particles)
+// from the sub-tile boxes: lane s classifies sub-tile s, a ballot gathers the
+// warp-uniform mask, and runs of far sub-tiles take the packed loop while
+// near (or coarse-scale) sub-tiles take the scalar double-float path.
 template <int BLOCK, int IPT>
 __device__ __forceinline__ void r3x2_tile(const MixedArgs &a, int J, const float *sxb, const float *seb,
-                                          const uint32_t *sidb, const float4 *sresb, float4 mI0, float4 wc, float4 wh,
-                                          const float *xi, const float *yi, const float *zi, const float *ei,
-                                          const float *lx, const float *ly, const float *lz, const uint32_t *ii,
-                                          double *ax, double *ay, double *az)
+                                          const uint32_t *sidb, const float4 *sresb, const float4 *ssubb, float4 mI0,
+                                          float4 wc, float4 wh,
+                                          float wemax, const float *xi, const float *yi, const float *zi,
+                                          const float *ei, const float *lx, const float *ly, const float *lz,
+                                          const uint32_t *ii, double *ax, double *ay, double *az)
 {
     constexpr int T = BLOCK * IPT;
+    constexpr int NS = T / SUBTILE;  // 4 .. 32 sub-tiles
+    constexpr unsigned ALL = NS == 32 ? 0xffffffffu : (1u << NS) - 1u;
     const float4 mJ0 = __ldg(a.jmeta + 2 * J);
-    const float4 mJ1 = __ldg(a.jmeta + 2 * J + 1);
     float eOx, eOy, eOz;
     const float dOx = two_diff(mJ0.x, mI0.x, eOx), dOy = two_diff(mJ0.y, mI0.y, eOy),
                 dOz = two_diff(mJ0.z, mI0.z, eOz);
-    // Near field / coarse FP32 scale, decided per warp (warp-uniform
-    // branch): in a near tile pair, warps away from J keep the far loop.
-    const bool full = warp_full(dOx, dOy, dOz, wc, wh, mJ1, mI0.w + mJ0.w, a.guard2);
+    // Near field / coarse FP32 scale per (warp, sub-tile), warp-uniform.
+    const int lane = threadIdx.x & 31;
+    bool f = false;
+    if (lane < NS) f = warp_full_sub(dOx, dOy, dOz, ssubb[2 * lane], ssubb[2 * lane + 1], wc, wh, wemax, a.guard2);
+    const unsigned full = __ballot_sync(0xffffffffu, f) & ALL;
     const float *X = sxb;
     const float *Y = X + T;
     const float *Z = X + 2 * T;
     const float *Mq = X + 3 * T;
 
-    if (!full) {
-        f2 PX[IPT], PY[IPT], PZ[IPT], AX[IPT], AY[IPT], AZ[IPT];
-#pragma unroll
-        for (int k = 0; k < IPT; k++) {
-            PX[k] = f2_bcast(((xi[k] - dOx) - eOx) + lx[k]);
-            PY[k] = f2_bcast(((yi[k] - dOy) - eOy) + ly[k]);
-            PZ[k] = f2_bcast(((zi[k] - dOz) - eOz) + lz[k]);
-            AX[k] = AY[k] = AZ[k] = 0ull;  // {+0, +0}
-        }
-#pragma unroll 2
-        for (int jj = 0; jj < T; jj += 4) {
-            const ulonglong2 qx4 = *reinterpret_cast<const ulonglong2 *>(X + jj);
-            const ulonglong2 qy4 = *reinterpret_cast<const ulonglong2 *>(Y + jj);
-            const ulonglong2 qz4 = *reinterpret_cast<const ulonglong2 *>(Z + jj);
-            const ulonglong2 qm4 = *reinterpret_cast<const ulonglong2 *>(Mq + jj);
-#pragma unroll
-            for (int h = 0; h < 2; h++) {
-                const f2 qx = h ? qx4.y : qx4.x, qy = h ? qy4.y : qy4.x, qz = h ? qz4.y : qz4.x;
-                const f2 qm = h ? qm4.y : qm4.x;
-#pragma unroll
-                for (int k = 0; k < IPT; k++) {
-                    const f2 dx = f2_sub(qx, PX[k]), dy = f2_sub(qy, PY[k]), dz = f2_sub(qz, PZ[k]);
-                    const f2 r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx)));
-                    float r2a, r2b;
-                    f2_unpack(r2, r2a, r2b);
-                    const f2 ri = f2_pack(rsqrt_mufu(r2a), rsqrt_mufu(r2b));
-                    const f2 w = f2_mul(f2_mul(qm, ri), f2_mul(ri, ri));
-                    AX[k] = f2_fma(w, dx, AX[k]);
-                    AY[k] = f2_fma(w, dy, AY[k]);
-                    AZ[k] = f2_fma(w, dz, AZ[k]);
-                }
-            }
-        }
-#pragma unroll
-        for (int k = 0; k < IPT; k++) {
-            float l0, l1;
-            f2_unpack(AX[k], l0, l1);
-            ax[k] += (double)(l0 + l1);
-            f2_unpack(AY[k], l0, l1);
-            ay[k] += (double)(l0 + l1);
-            f2_unpack(AZ[k], l0, l1);
-            az[k] += (double)(l0 + l1);
-        }
-    } else {
-        // Near field: scalar double-float path with the spline
-        // (StePS/src/forces.cc:52-87); the self pair gets d = 0.
-        float phx[IPT], phy[IPT], phz[IPT], plx[IPT], ply[IPT], plz[IPT], fx[IPT], fy[IPT], fz[IPT];
-#pragma unroll
-        for (int k = 0; k < IPT; k++) {
-            frame_split(xi[k], lx[k], dOx, eOx, phx[k], plx[k]);
-            frame_split(yi[k], ly[k], dOy, eOy, phy[k], ply[k]);
-            frame_split(zi[k], lz[k], dOz, eOz, phz[k], plz[k]);
-            fx[k] = fy[k] = fz[k] = 0.0f;
-        }
-        for (int jj = 0; jj < T; ++jj) {
-            const float qx = X[jj], qy = Y[jj], qz = Z[jj], qm = Mq[jj];
-            const float ej = seb[jj];
-            const uint32_t jid = sidb[jj];
-            const float4 ql = sresb[jj];
+    // Segments of consecutive sub-tiles with the same decision, in order;
+    // each takes one path and folds its FP32 sums into the FP64 accumulators.
+    unsigned rem = ALL;
+    while (rem) {
+        const int s0 = __ffs(rem) - 1;
+        const bool nearseg = (full >> s0) & 1u;
+        const unsigned same = (nearseg ? full : ~full) & ALL;
+        const unsigned rest = ~(same >> s0);
+        const int s1 = rest ? s0 + __ffs(rest) - 1 : 32;
+        rem = s1 >= 32 ? 0u : rem & ~((1u << s1) - 1u);
+        // The frame offsets pass through a move that depends on the segment,
+        // so neither path's set-up is hoisted out of this loop (both would
+        // then stay live across the other path and cost registers).
+        const float oX = pin_to(dOx, s0), oY = pin_to(dOy, s0), oZ = pin_to(dOz, s0);
+        if (!nearseg) {
+            // Far field: packed FP32x2.
+            f2 PX[IPT], PY[IPT], PZ[IPT], AX[IPT], AY[IPT], AZ[IPT];
 #pragma unroll
             for (int k = 0; k < IPT; k++) {
-                const bool self = jid == ii[k];
-                const float dx = self ? 0.0f : (qx - phx[k]) + (ql.x - plx[k]);
-                const float dy = self ? 0.0f : (qy - phy[k]) + (ql.y - ply[k]);
-                const float dz = self ? 0.0f : (qz - phz[k]) + (ql.z - plz[k]);
-                const float b = ei[k] + ej;
-                const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                const float ri = rsqrt_mufu(r2);
-                float w = ri * ri * ri;
-                if (r2 < b * b) w = spline_inner_f32(r2, b);
-                w *= qm;
-                fx[k] = fmaf(w, dx, fx[k]);
-                fy[k] = fmaf(w, dy, fy[k]);
-                fz[k] = fmaf(w, dz, fz[k]);
+                PX[k] = f2_bcast(((xi[k] - oX) - eOx) + lx[k]);
+                PY[k] = f2_bcast(((yi[k] - oY) - eOy) + ly[k]);
+                PZ[k] = f2_bcast(((zi[k] - oZ) - eOz) + lz[k]);
+                AX[k] = AY[k] = AZ[k] = 0ull;  // {+0, +0}
+            }
+#pragma unroll 2
+            for (int jj = s0 * SUBTILE; jj < s1 * SUBTILE; jj += 4) {
+                const ulonglong2 qx4 = *reinterpret_cast<const ulonglong2 *>(X + jj);
+                const ulonglong2 qy4 = *reinterpret_cast<const ulonglong2 *>(Y + jj);
+                const ulonglong2 qz4 = *reinterpret_cast<const ulonglong2 *>(Z + jj);
+                const ulonglong2 qm4 = *reinterpret_cast<const ulonglong2 *>(Mq + jj);
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const f2 qx = h ? qx4.y : qx4.x, qy = h ? qy4.y : qy4.x, qz = h ? qz4.y : qz4.x;
+                    const f2 qm = h ? qm4.y : qm4.x;
+#pragma unroll
+                    for (int k = 0; k < IPT; k++) {
+                        const f2 dx = f2_sub(qx, PX[k]), dy = f2_sub(qy, PY[k]), dz = f2_sub(qz, PZ[k]);
+                        const f2 r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx)));
+                        float r2a, r2b;
+                        f2_unpack(r2, r2a, r2b);
+                        const f2 ri = f2_pack(rsqrt_mufu(r2a), rsqrt_mufu(r2b));
+                        const f2 w = f2_mul(f2_mul(qm, ri), f2_mul(ri, ri));
+                        AX[k] = f2_fma(w, dx, AX[k]);
+                        AY[k] = f2_fma(w, dy, AY[k]);
+                        AZ[k] = f2_fma(w, dz, AZ[k]);
+                    }
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < IPT; k++) {
+                float l0, l1;
+                f2_unpack(AX[k], l0, l1);
+                ax[k] += (double)(l0 + l1);
+                f2_unpack(AY[k], l0, l1);
+                ay[k] += (double)(l0 + l1);
+                f2_unpack(AZ[k], l0, l1);
+                az[k] += (double)(l0 + l1);
+            }
+        } else {
+            // Near field: scalar double-float path with the spline
+            // (StePS/src/forces.cc:52-87); the self pair gets d = 0.
+            float phx[IPT], phy[IPT], phz[IPT], plx[IPT], ply[IPT], plz[IPT], fx[IPT], fy[IPT], fz[IPT];
+#pragma unroll
+            for (int k = 0; k < IPT; k++) {
+                frame_split(xi[k], lx[k], oX, eOx, phx[k], plx[k]);
+                frame_split(yi[k], ly[k], oY, eOy, phy[k], ply[k]);
+                frame_split(zi[k], lz[k], oZ, eOz, phz[k], plz[k]);
+                fx[k] = fy[k] = fz[k] = 0.0f;
+            }
+            for (int jj = s0 * SUBTILE; jj < s1 * SUBTILE; ++jj) {
+                const float qx = X[jj], qy = Y[jj], qz = Z[jj], qm = Mq[jj];
+                const float ej = seb[jj];
+                const uint32_t jid = sidb[jj];
+                const float4 ql = sresb[jj];
+#pragma unroll
+                for (int k = 0; k < IPT; k++) {
+                    const bool self = jid == ii[k];
+                    const float dx = self ? 0.0f : (qx - phx[k]) + (ql.x - plx[k]);
+                    const float dy = self ? 0.0f : (qy - phy[k]) + (ql.y - ply[k]);
+                    const float dz = self ? 0.0f : (qz - phz[k]) + (ql.z - plz[k]);
+                    const float b = ei[k] + ej;
+                    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                    const float ri = rsqrt_mufu(r2);
+                    float w = ri * ri * ri;
+                    if (r2 < b * b) w = spline_inner_f32(r2, b);
+                    w *= qm;
+                    fx[k] = fmaf(w, dx, fx[k]);
+                    fy[k] = fmaf(w, dy, fy[k]);
+                    fz[k] = fmaf(w, dz, fz[k]);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < IPT; k++) {
+                ax[k] += (double)fx[k];
+                ay[k] += (double)fy[k];
+                az[k] += (double)fz[k];
             }
         }
-#pragma unroll
-        for (int k = 0; k < IPT; k++) {
-            ax[k] += (double)fx[k];
-            ay[k] += (double)fy[k];
-            az[k] += (double)fz[k];
-        }
     }
+}
+
+// Largest softening length of this warp's i particles.
+template <int IPT>
+__device__ __forceinline__ float warp_eps_max(const float *ei)
+{
+    float e = ei[0];
+#pragma unroll
+    for (int k = 1; k < IPT; k++) e = fmaxf(e, ei[k]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) e = fmaxf(e, __shfl_xor_sync(0xffffffffu, e, o));
+    return e;
 }
 
 template <int BLOCK, int IPT, bool LIST>
@@ -156,6 +204,7 @@ __device__ __forceinline__ void r3x2_body(const MixedArgs &a)
     __shared__ __align__(16) float se[2][T];
     __shared__ __align__(16) uint32_t sid[2][T];
     __shared__ __align__(16) float4 sres[2][T];
+    __shared__ __align__(16) float4 ssub[2][2 * (T / SUBTILE)];
     __shared__ int s_item;
     const int tid = threadIdx.x;
 
@@ -174,8 +223,8 @@ __device__ __forceinline__ void r3x2_body(const MixedArgs &a)
             J1 = d.z;
             base = (size_t)d.w * 3 * T;
         } else {
-            I = item / a.S;
-            const int chunk = item - I * a.S;
+            I = (item / a.S) * a.istride;
+            const int chunk = item % a.S;
             J0 = chunk * a.tpc;
             J1 = min(a.njt, J0 + a.tpc);
             base = (size_t)chunk * a.part_stride + 3 * (size_t)I * T;
@@ -204,20 +253,21 @@ __device__ __forceinline__ void r3x2_body(const MixedArgs &a)
 
         float4 wc, wh;  // this warp's i box in I's frame
         warp_box<IPT>(xi, yi, zi, wc, wh);
+        const float wemax = warp_eps_max<IPT>(ei);
 
-        if (J0 < J1) stage_soa<BLOCK, IPT>(a, J0, sx[0], se[0], sid[0], sres[0]);
+        if (J0 < J1) stage_soa<BLOCK, IPT>(a, J0, sx[0], se[0], sid[0], sres[0], ssub[0]);
         for (int J = J0; J < J1; ++J) {
             const int buf = (J - J0) & 1;
             if (J + 1 < J1) {
-                stage_soa<BLOCK, IPT>(a, J + 1, sx[buf ^ 1], se[buf ^ 1], sid[buf ^ 1], sres[buf ^ 1]);
+                stage_soa<BLOCK, IPT>(a, J + 1, sx[buf ^ 1], se[buf ^ 1], sid[buf ^ 1], sres[buf ^ 1], ssub[buf ^ 1]);
                 cp_wait<1>();
             } else {
                 cp_wait<0>();
             }
             __syncthreads();
 
-            r3x2_tile<BLOCK, IPT>(a, J, sx[buf], se[buf], sid[buf], sres[buf], mI0, wc, wh, xi, yi, zi, ei, lx, ly, lz,
-                                  ii, ax, ay, az);
+            r3x2_tile<BLOCK, IPT>(a, J, sx[buf], se[buf], sid[buf], sres[buf], ssub[buf], mI0, wc, wh, wemax, xi, yi,
+                                  zi, ei, lx, ly, lz, ii, ax, ay, az);
             __syncthreads();
         }
 
@@ -247,11 +297,14 @@ __device__ __forceinline__ void r3x2_pipe_body(const MixedArgs &a)
     constexpr int T = BLOCK * IPT;
     constexpr int S = T <= 256 ? 4 : 2;
     constexpr int NW = BLOCK / 32;
-    constexpr unsigned BYTES = 40u * T;  // SoA 16T + softening 4T + ids 4T + residuals 16T
+    constexpr int NS2 = 2 * (T / SUBTILE);
+    // SoA 16T + softening 4T + ids 4T + residuals 16T + sub-tile boxes 2T
+    constexpr unsigned BYTES = 40u * T + 16u * NS2;
     __shared__ __align__(128) float sx[S][4 * T];  // per stage X[T], Y[T], Z[T], M[T]
     __shared__ __align__(16) float se[S][T];
     __shared__ __align__(16) uint32_t sid[S][T];
     __shared__ __align__(16) float4 sres[S][T];
+    __shared__ __align__(16) float4 ssub[S][NS2];
     __shared__ __align__(8) unsigned long long full[S], empty[S];
     __shared__ int s_item, s_abort;
     const int tid = threadIdx.x, lane = tid & 31;
@@ -276,6 +329,7 @@ __device__ __forceinline__ void r3x2_pipe_body(const MixedArgs &a)
             bulk_g2s(se[st], a.jeps + (size_t)J * T, 4u * T, &full[st]);
             bulk_g2s(sid[st], a.jidx + (size_t)J * T, 4u * T, &full[st]);
             bulk_g2s(sres[st], a.jres + (size_t)J * T, 16u * T, &full[st]);
+            bulk_g2s(ssub[st], a.jsub + (size_t)J * NS2, 16u * NS2, &full[st]);
         }
         issued++;
         return true;
@@ -291,8 +345,8 @@ __device__ __forceinline__ void r3x2_pipe_body(const MixedArgs &a)
         __syncthreads();
         const int item = s_item;
         if (item >= a.nitems) break;
-        const int I = item / a.S;
-        const int chunk = item - I * a.S;
+        const int I = (item / a.S) * a.istride;
+        const int chunk = item % a.S;
         const int J0 = chunk * a.tpc;
         const int J1 = min(a.njt, J0 + a.tpc);
         const size_t base = (size_t)chunk * a.part_stride + 3 * (size_t)I * T;
@@ -318,6 +372,7 @@ __device__ __forceinline__ void r3x2_pipe_body(const MixedArgs &a)
         }
         float4 wc, wh;
         warp_box<IPT>(xi, yi, zi, wc, wh);
+        const float wemax = warp_eps_max<IPT>(ei);
 
         bool ok = true;
         if (tid == 0)
@@ -332,8 +387,8 @@ __device__ __forceinline__ void r3x2_pipe_body(const MixedArgs &a)
                 if (lane == 0) abort_block();
                 break;
             }
-            r3x2_tile<BLOCK, IPT>(a, J, sx[st], se[st], sid[st], sres[st], mI0, wc, wh, xi, yi, zi, ei, lx, ly, lz, ii,
-                                  ax, ay, az);
+            r3x2_tile<BLOCK, IPT>(a, J, sx[st], se[st], sid[st], sres[st], ssub[st], mI0, wc, wh, wemax, xi, yi, zi, ei,
+                                  lx, ly, lz, ii, ax, ay, az);
             __syncwarp();
             if (lane == 0) mbar_arrive(&empty[st]);
             consumed++;
@@ -360,8 +415,11 @@ __global__ void __launch_bounds__(BLOCK) k_pair_r3x2_pipe(MixedArgs a)
     r3x2_pipe_body<BLOCK, IPT>(a);
 }
 
+// Default packed kernel: for blocks of 64 or 128 threads with up to two i
+// particles a thread, at least 640 resident threads per SM asked of the
+// register allocator (102 registers a thread).
 template <int BLOCK, int IPT, bool LIST>
-__global__ void __launch_bounds__(BLOCK) k_pair_r3x2(MixedArgs a)
+__global__ void __launch_bounds__(BLOCK, BLOCK <= 128 && IPT <= 2 ? 640 / BLOCK : 1) k_pair_r3x2(MixedArgs a)
 {
     r3x2_body<BLOCK, IPT, LIST>(a);
 }

@@ -132,8 +132,8 @@ __global__ void __launch_bounds__(BLOCK) k_pair_t3(MixedArgs a)
         __syncthreads();
         const int item = s_item;
         if (item >= a.nitems) return;
-        const int I = item / a.S;
-        const int chunk = item - I * a.S;
+        const int I = (item / a.S) * a.istride;
+        const int chunk = item % a.S;
         const int J0 = chunk * a.tpc;
         const int J1 = min(a.njt, J0 + a.tpc);
 
@@ -517,8 +517,8 @@ __global__ void __launch_bounds__(BLOCK) k_pair_s1tab(MixedArgs a)
         __syncthreads();
         const int item = s_item;
         if (item >= a.nitems) return;
-        const int I = item / a.S;
-        const int chunk = item - I * a.S;
+        const int I = (item / a.S) * a.istride;
+        const int chunk = item % a.S;
         const int J0 = chunk * a.tpc;
         const int J1 = min(a.njt, J0 + a.tpc);
 

@@ -10,7 +10,19 @@ import subprocess
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF_SRC = "/root/reference/StePS/src"
+
+
+def _ref_src():
+    """The reference source directory oracle/Makefile's `ref` target was built
+    from (it records it in oracle/_ref/ref_src.txt); "" when not built here."""
+    try:
+        with open(os.path.join(ROOT, "oracle", "_ref", "ref_src.txt")) as f:
+            return f.read().strip()
+    except OSError:
+        return ""
+
+
+REF_SRC = _ref_src()
 LIB_DIR = os.path.join(ROOT, "steps_gb300", "_build")
 
 VARIANTS = {
@@ -21,7 +33,7 @@ VARIANTS = {
 }
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_SRC), reason="reference tree not present")
+@pytest.mark.skipif(not REF_SRC or not os.path.isdir(REF_SRC), reason="reference tree not present")
 @pytest.mark.parametrize("variant", sorted(VARIANTS))
 def test_reference_driver_links_with_shim(tmp_path, variant):
     if not os.path.exists(os.path.join(LIB_DIR, "libsteps_gb300.so")):
