@@ -22,6 +22,15 @@ compiled unmodified into oracle/_ref/*.cubin) with the reference's launch
 shape, in its FP32 and FP64 builds, on one full wave of i particles against a
 j subset sized to about --ref-seconds per launch.
 
+The default run (cfg1 at one GPU) also measures every other workload in a
+`configs` block of the same JSON line -- cfg0, cfg2 with the image sum and
+with the (rho, z) table at orders 0/2/4, cfg3 at orders 2/4 and on the
+IS_PERIODIC = 3 table (Ng = 127), cfg4 graph against plain launches -- each
+with its pair rate, issue-roofline fraction, FP64 rate, p50/p99/max against
+FP64 and a short CPU baseline; and a `ref_gpu` block timing the reference's
+own CUDA kernels (FP32 and FP64 builds) on the R^3, T^3 and S1xR2 workloads.
+--no-configs skips both.
+
 With --gpus N > 1 (torchrun) every rank evaluates its own independent
 realisation (seed + rank): weak scaling, no collective on the data path.
 """
@@ -48,10 +57,11 @@ UNIT = "pairs/s"
 # (index radius 3), k vectors |k| <= 5 (2 pi / L) (index radius 6).
 T3_NG = 63
 LOOPS = ["fp32", "fp32x2", "fp32x2 (768 threads/SM)", "fp32x2 (1024 threads/SM)", "fp32x2, bulk-copy mbarrier pipeline"]
-# DRAM bytes (read + write) of one launch of the pair kernel, from a one-pass ncu
-# capture of dram__bytes_read.sum + dram__bytes_write.sum (profiles/launches_r3_n1048576.md):
-# N = 2^20 R^3, 256x1 packed at 768 threads/SM, 64 j chunks.
-NCU_TRAFFIC = {("cfg1", 1 << 20): 104.15e6 + 1.60e9}
+# DRAM bytes (read + write) of one launch of the pair kernel, from one-pass ncu
+# captures of dram__bytes_read.sum + dram__bytes_write.sum, keyed by
+# (workload, N, threads, ipt, pair-loop variant): the traffic is reported only
+# for the shape that was timed, else null.
+NCU_TRAFFIC = {}
 
 
 def parse():
@@ -80,6 +90,10 @@ def parse():
                     help="R^3 pair loop without autotuning: 0 fp32, 1 fp32x2, 2/3 fp32x2 at 768/1024 threads per SM, "
                          "4 fp32x2 with the bulk-copy pipeline")
     ap.add_argument("--shape", default="", help="kernel shape THREADSxIPT without autotuning, e.g. 128x1")
+    ap.add_argument("--t3-level", type=int, default=0,
+                    help="cfg3: Ewald table of the reference's IS_PERIODIC level 3 (Ng = 127, rel_cut 3.6, rec_cut 10) "
+                         "instead of the workload's Ng = 63 table")
+    ap.add_argument("--no-configs", action="store_true", help="skip the configs and ref_gpu blocks")
     return ap.parse_args()
 
 
@@ -122,8 +136,16 @@ def workload(args, rank=0):
         return ps, p, 11 + 11 * 7, f"S1xR2 N={n} L_z=200 Mpc R_max=600 Mpc, 7 z images (IS_PERIODIC=2)", None
     n = args.n or (1 << 19)
     ps = W.t3_clumpy(n, 100.0, seed=3 + rank)
-    p = S.params(S.T3, is_periodic=2, L=100.0, rsim=50.0, ewald_order=args.order)
     flops = 33 + (494 if args.order == 4 else 62)
+    if getattr(args, "t3_level", 0) == 3:
+        # The reference's IS_PERIODIC = 3 table (StePS/src/main.cc:433-440):
+        # Ng = 127, alpha = 2/L, rel_cut 3.6, rec_cut 10 over ewald_space(rel_cut + 1)
+        # and ewald_space(rec_cut + 2).
+        p = S.params(S.T3, is_periodic=3, L=100.0, rsim=50.0, ewald_order=args.order)
+        table = {"kind": "t3", "args": (127, 100.0, 2.0 / 100.0, 3.6, 10.0, 4.6, 12.0)}
+        return ps, p, flops, (f"T3 N={n} L=100 Mpc clumpy, IS_PERIODIC=3 Ewald table Ng=127 (rel_cut 3.6, rec_cut 10) "
+                              f"order {args.order}"), table
+    p = S.params(S.T3, is_periodic=2, L=100.0, rsim=50.0, ewald_order=args.order)
     table = {"kind": "t3", "args": (T3_NG, 100.0, 2.0 / 100.0, 2.0, 5.0 * 2.0 * math.pi / 100.0, 3.0, 6.0)}
     return ps, p, flops, f"T3 N={n} L=100 Mpc clumpy, Ewald table Ng={T3_NG} order {args.order}", table
 
@@ -298,27 +320,21 @@ def set_ref_table(k, tab):
         k.set_table_s1r2(tab[0], tab[2], tab[3])
 
 
-def run_reference_gpu(args, ws, rank):
-    """The reference's CUDA kernels (oracle/refgpu.py) on this workload: FP32
+def ref_gpu_measure(args, ps, p, flops, desc, table, seconds, steps, warmup):
+    """The reference's CUDA kernels (oracle/refgpu.py) on one workload: FP32
     build (USE_SINGLE_PRECISION) and FP64 build, kernel time only, with the
-    FP32 build's error against the FP64 build on the same sample."""
-    if rank != 0:
-        return
+    FP32 build's error against the FP64 build on the same sample. None when the
+    cubins were not built."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import refgpu
 
-    ps, p, flops, desc, table = workload(args)
     base = {0: "r3", 1: "t3", 2: "s1nl"}[p.topology]
     if p.topology == 1:
-        flops = 33 + 494  # tricubic
+        flops = 33 + 494  # the reference GPU kernel interpolates T^3 tricubically only
     if table and table["kind"] == "s1":
         base = f"s1o{p.ewald_order}"
-    why = None
     if not (refgpu.available(base) and refgpu.available(base + "sp")):
-        why = "oracle/_ref/forces_cuda_*.cubin not built (needs the reference tree at build time)"
-    if why:
-        print(json.dumps({"impl": "reference", "device": "gpu", "unavailable": why}), flush=True)
-        return
+        return None
     kw = {}
     if p.topology == 1:
         kw = {"is_periodic": p.is_periodic, "L": p.L}
@@ -333,8 +349,8 @@ def run_reference_gpu(args, ws, rank):
         ni = min(ps.n, k.wave())
         nj = min(ps.n, 1024)
         ms, _ = k.time(0, ni - 1, nj, steps=1, warmup=1, **kw)  # calibration
-        nj = int(min(ps.n, max(nj, nj * args.ref_seconds * 1e3 / max(ms, 1e-3))))
-        ms, F = k.time(0, ni - 1, nj, steps=args.steps, warmup=args.warmup, **kw)
+        nj = int(min(ps.n, max(nj, nj * seconds * 1e3 / max(ms, 1e-3))))
+        ms, F = k.time(0, ni - 1, nj, steps=steps, warmup=warmup, **kw)
         res[v] = {"pairs_per_s": ni * nj / (ms * 1e-3), "kernel_ms": ms, "i": ni, "j": nj, "F": F,
                   "registers": k.registers, "blocks_per_sm": k.blocks_per_sm}
     a, b = res[base + "sp"], res[base]
@@ -347,61 +363,84 @@ def run_reference_gpu(args, ws, rank):
         set_ref_table(k, tab)
         Fa = k.forces(0, b["i"] - 1, b["j"], **kw)
     rel = np.linalg.norm(Fa - Fb, axis=1) / np.maximum(np.linalg.norm(Fb, axis=1), 1e-300)
-    v = a["pairs_per_s"]
     interp = ", tricubic (the reference GPU kernel's only T^3 interpolation)" if p.topology == 1 else ""
+    return {"workload": desc + interp, "kernel": base, "flops_per_pair": flops,
+            "sample": f"i = one full wave of resident blocks ({a['i']}), j = the first {a['j']} particles "
+                      f"(FP64 build: {b['j']}); pair cost does not depend on N",
+            "fp32_build": {k_: a[k_] for k_ in ("pairs_per_s", "kernel_ms", "i", "j", "registers", "blocks_per_sm")},
+            "fp64_build": {k_: b[k_] for k_ in ("pairs_per_s", "kernel_ms", "i", "j", "registers", "blocks_per_sm")},
+            "accuracy_fp32_vs_fp64": {"p50": float(np.percentile(rel, 50)), "p99": float(np.percentile(rel, 99)),
+                                      "max": float(rel.max()), "sample": f"{b['i']} i x {b['j']} j"}}
+
+
+def run_reference_gpu(args, ws, rank):
+    """--impl reference --ref-device gpu: the reference's CUDA kernels on the
+    chosen workload, as its own JSON line."""
+    if rank != 0:
+        return
+    ps, p, flops, desc, table = workload(args)
+    r = ref_gpu_measure(args, ps, p, flops, desc, table, args.ref_seconds, args.steps, args.warmup)
+    if r is None:
+        print(json.dumps({"impl": "reference", "device": "gpu", "unavailable":
+                          "oracle/_ref/forces_cuda_*.cubin not built (needs the reference tree at build time)"}),
+              flush=True)
+        return
+    a = r["fp32_build"]
+    v = a["pairs_per_s"]
     line = {"impl": "reference", "device": "gpu", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": a["kernel_ms"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 (the reference's USE_SINGLE_PRECISION build)",
             "data": "synthetic (seeded)",
-            "config": {"workload": desc + interp,
-                       "sample": f"i = one full wave of resident blocks ({a['i']}), j = the first {a['j']} "
-                                 f"particles (FP64 build: {b['j']}); pair cost does not depend on N",
+            "config": {"workload": r["workload"], "sample": r["sample"],
                        "launch": "32 x SMs blocks of 256 threads, grid-stride i loop (StePS/src/forces_cuda.cu:1053)",
                        "source": "StePS/src/forces_cuda.cu compiled unmodified for sm_103a (nvcc -O3)"},
-            "roofline": {"bound": "fp32", "achieved": v * flops / 1e12, "unit": "TFLOP/s",
-                         "flops_per_pair": flops},
-            "fp32_build": {k_: a[k_] for k_ in ("pairs_per_s", "kernel_ms", "i", "j", "registers", "blocks_per_sm")},
-            "fp64_build": {k_: b[k_] for k_ in ("pairs_per_s", "kernel_ms", "i", "j", "registers", "blocks_per_sm")},
-            "accuracy_fp32_vs_fp64": {"p50": float(np.percentile(rel, 50)), "p99": float(np.percentile(rel, 99)),
-                                      "max": float(rel.max()), "sample": f"{b['i']} i x {b['j']} j"},
+            "roofline": {"bound": "fp32", "achieved": v * r["flops_per_pair"] / 1e12, "unit": "TFLOP/s",
+                         "flops_per_pair": r["flops_per_pair"]},
+            "fp32_build": a, "fp64_build": r["fp64_build"], "accuracy_fp32_vs_fp64": r["accuracy_fp32_vs_fp64"],
             "e2e": None, "e2e_note": "kernel time only; the reference wrapper's per-call allocations and copies "
                                      "(forces_cuda.cu:976-1105) are not timed"}
     print(json.dumps(line), flush=True)
 
 
-def run_ours(args, ws, rank, local, dist):
-    import steps_gb300 as S
+def nominal_fp32_peak(sm_mhz):
+    """FP32 FMA issue peak from the device's SM count and the sampled SM clock
+    (128 FP32 lanes per SM, an FMA counted as 2 flops), TFLOP/s."""
+    try:
+        import torch
 
-    ps, p, flops, desc, table = workload(args, rank)
-    n = ps.n
-    eng = S.Engine(local)
+        nsm = torch.cuda.get_device_properties(0).multi_processor_count
+    except Exception:
+        return None, None
+    if not sm_mhz:
+        return None, nsm
+    return nsm * 128 * 2 * sm_mhz * 1e6 / 1e12, nsm
+
+
+def setup_engine_workload(eng, ps, table):
     eng.set_particles(ps.m, ps.eps)
     if table and table["kind"] == "t3":
         eng.build_table_t3(*table["args"])
     elif table:
         eng.build_table_s1r2(*table["args"])
     eng.upload_positions(ps.x)
-    f32_peak, f64_peak = eng.measure_peaks()
-    if args.variant >= 0:
-        eng.set_variant(args.variant)
-    if args.shape:
-        th, ipt = (int(v) for v in args.shape.split("x"))
-        eng.set_tuning(th, ipt, 0)
-    fixed = args.no_autotune or args.variant >= 0 or bool(args.shape)
-    shape = None if fixed else eng.autotune(p)
 
-    for _ in range(args.warmup):
+
+def measure(eng, S, ps, p, flops, table, steps, warmup, fp64_sample, f32_peak, f64_peak, shape_fixed=False,
+            flush=True):
+    """One workload on the resident engine: autotune (unless the shape is
+    fixed), warm-up, `steps` timed force evaluations (CUDA events on the
+    library stream, L2 flushed between them), the FP64 kernel on an i sample
+    and the mixed kernel's error against it. Positions must be resident."""
+    n = ps.n
+    shape = None if shape_fixed else eng.autotune(p)
+    for _ in range(warmup):
         eng.forces_resident(p, S.MIXED)
-    eng.synchronize()
-
-    clocks = ClockSampler(local)
-    clocks.start()
-    barrier(dist)
     eng.synchronize()
     launches0 = eng.launch_count()
     step_ms, kernel_ms, prep_ms = [], [], []
-    for _ in range(args.steps):
-        eng.flush_l2(512 << 20)  # evict L2 (129 MB) between steps; outside the step's events
+    for _ in range(steps):
+        if flush:
+            eng.flush_l2(512 << 20)  # evict L2 (129 MB) between steps; outside the step's events
         eng.mark(0)
         eng.forces_resident(p, S.MIXED)
         eng.mark(1)
@@ -409,32 +448,12 @@ def run_ours(args, ws, rank, local, dist):
         prep_ms.append(eng.phase_ms(0))
         kernel_ms.append(eng.phase_ms(1))
     eng.synchronize()
-    launches = eng.launch_count() - launches0  # our kernels only (the L2 flush is a memset)
-    barrier(dist)
-    clk = clocks.stop()
-    total_ms = allmax(dist, float(sum(step_ms)))
+    launches = eng.launch_count() - launches0
     pairs_step = float(n) * float(n)
-    value = ws * pairs_step * args.steps / (total_ms * 1e-3)
     kern_ms = float(np.mean(kernel_ms))
     kern_rate = pairs_step / (kern_ms * 1e-3)
     Fmixed = eng.download_forces(n)
-
-    # e2e through the host-buffer C-ABI call (H2D positions, D2H forces inside),
-    # the host arrays in page-locked memory.
-    x_pin = eng.host_array(ps.x.shape)
-    x_pin[...] = ps.x
-    F_host = eng.host_array((n, 3))
-    e2e_s = []
-    for _ in range(args.e2e_steps):
-        barrier(dist)
-        t0 = time.perf_counter()
-        eng.forces(x_pin, p, S.MIXED, out=F_host)
-        e2e_s.append(time.perf_counter() - t0)
-    e2e_t = allmax(dist, float(np.mean(e2e_s)))
-    e2e_value = ws * pairs_step / e2e_t
-
-    # FP64 kernel on an i subset (cost is linear in the i range) + accuracy.
-    fs = min(args.fp64_sample, n)
+    fs = min(fp64_sample, n)
     lo = n // 2 - fs // 2
     hi = lo + fs - 1
     eng.forces_resident(p, S.FP64, lo, hi)
@@ -443,59 +462,129 @@ def run_ours(args, ws, rank, local, dist):
     F64 = eng.download_forces(hi - lo + 1)
     f64_rate = fs * n / (f64_ms * 1e-3)
     rel = np.linalg.norm(Fmixed[lo:hi + 1] - F64, axis=1) / np.linalg.norm(F64, axis=1)
-    acc = {"p50": float(np.percentile(rel, 50)), "p99": float(np.percentile(rel, 99)), "max": float(rel.max()),
-           "sample": f"{fs} i particles vs the FP64 kernel"}
-
     achieved = kern_rate * flops / 1e12
-    nominal = 152 * 128 * 2 * 2070e6 / 1e12
-    line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": float(np.mean(step_ms)), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 pairs / f64 accumulate (positions f64)", "data": "synthetic (seeded; no public dataset)",
-        "config": {"workload": desc + ", one full force evaluation per step", "n": n, "pairs_per_step": pairs_step,
-                   "parallelism": "one independent realisation per GPU" if ws > 1 else "1 GPU",
-                   "l2": "512 MB flush between steps", "precision": "mixed",
-                   "kernel_shape": ({"threads": shape[0], "ipt": shape[1], "pair_loop": LOOPS[shape[2]]}
-                                    if shape else (args.shape or "128x2") + " " + LOOPS[max(args.variant, 0)]),
-                   "prep_ms": float(np.mean(prep_ms))},
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(x_pin.nbytes),
-                "d2h_bytes_per_step": int(F_host.nbytes), "ms_per_step": e2e_t * 1e3,
-                "host_memory": "page-locked (steps_gpu_host_alloc)"},
-        "roofline": {"bound": "fp32", "achieved": achieved, "peak": f32_peak / 1e12, "unit": "TFLOP/s",
-                     "frac": achieved / (f32_peak / 1e12),
-                     "traffic": NCU_TRAFFIC.get((args.workload, n)),
-                     "traffic_note": "DRAM bytes of one pair-kernel launch from an ncu capture (None: not captured "
-                                     "for this size); compute-bound, under 0.1 % of HBM bandwidth",
-                     "peak_kind": "FP32 FMA issue peak measured in this process (dependent-FMA-chain kernel)",
-                     "nominal_peak_at_max_clock": nominal, "frac_of_nominal": achieved / nominal,
-                     "flops_per_pair": flops, "kernel_ms": kern_ms},
+    return {
+        "step_ms": step_ms, "kernel_ms": kern_ms, "prep_ms": float(np.mean(prep_ms)), "kern_rate": kern_rate,
+        "value": pairs_step * steps / (float(sum(step_ms)) * 1e-3), "shape": shape, "launches": int(launches),
+        "achieved": achieved, "frac": achieved / (f32_peak / 1e12), "Fmixed": Fmixed,
         "fp64": {"pairs_per_s": f64_rate, "kernel_ms": f64_ms, "sample_i": fs,
                  "frac_of_fp64_peak": f64_rate * flops / f64_peak, "fp64_peak_tflops": f64_peak / 1e12},
         "speedup_vs_fp64": kern_rate / f64_rate,
-        "accuracy_mixed_vs_fp64": acc,
+        "accuracy": {"p50": float(np.percentile(rel, 50)), "p99": float(np.percentile(rel, 99)),
+                     "max": float(rel.max()), "sample": f"{fs} i particles vs the FP64 kernel"},
+    }
+
+
+def shape_desc(shape, args):
+    if shape:
+        return {"threads": shape[0], "ipt": shape[1], "pair_loop": LOOPS[shape[2]]}
+    return (args.shape or "128x2") + " " + LOOPS[max(args.variant, 0)]
+
+
+def traffic_of(workload_name, n, shape):
+    if not shape:
+        return None
+    return NCU_TRAFFIC.get((workload_name, n, shape[0], shape[1], shape[2]))
+
+
+def run_ours(args, ws, rank, local, dist):
+    import steps_gb300 as S
+
+    ps, p, flops, desc, table = workload(args, rank)
+    n = ps.n
+    eng = S.Engine(local)
+    setup_engine_workload(eng, ps, table)
+    f32_peak, f64_peak = eng.measure_peaks()
+    if args.variant >= 0:
+        eng.set_variant(args.variant)
+    if args.shape:
+        th, ipt = (int(v) for v in args.shape.split("x"))
+        eng.set_tuning(th, ipt, 0)
+    fixed = args.no_autotune or args.variant >= 0 or bool(args.shape)
+    shape_used = None
+    if args.shape and args.variant >= 0:
+        shape_used = (int(args.shape.split("x")[0]), int(args.shape.split("x")[1]), args.variant)
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(dist)
+    r = measure(eng, S, ps, p, flops, table, args.steps, args.warmup, args.fp64_sample, f32_peak, f64_peak,
+                shape_fixed=fixed)
+    barrier(dist)
+    clk = clocks.stop()
+    total_ms = allmax(dist, float(sum(r["step_ms"])))
+    pairs_step = float(n) * float(n)
+    value = ws * pairs_step * args.steps / (total_ms * 1e-3)
+    Fmixed = r["Fmixed"]
+
+    # e2e through the host-buffer C-ABI call (H2D positions, D2H forces inside),
+    # the host arrays in page-locked memory; and the same with ordinary
+    # (pageable) arrays, as the reference's driver hands over malloc memory.
+    x_pin = eng.host_array(ps.x.shape)
+    x_pin[...] = ps.x
+    F_host = eng.host_array((n, 3))
+    e2e_s, e2e_pg = [], []
+    for _ in range(args.e2e_steps):
+        barrier(dist)
+        t0 = time.perf_counter()
+        eng.forces(x_pin, p, S.MIXED, out=F_host)
+        e2e_s.append(time.perf_counter() - t0)
+    x_pg = np.array(ps.x, copy=True)
+    F_pg = np.empty((n, 3))
+    for _ in range(args.e2e_steps):
+        t0 = time.perf_counter()
+        eng.forces(x_pg, p, S.MIXED, out=F_pg)
+        e2e_pg.append(time.perf_counter() - t0)
+    e2e_t = allmax(dist, float(np.mean(e2e_s)))
+    e2e_value = ws * pairs_step / e2e_t
+
+    nominal, nsm = nominal_fp32_peak(clk.get("sm_mhz"))
+    achieved = r["achieved"]
+    timed_shape = r["shape"] or shape_used
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": float(np.mean(r["step_ms"])), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 pairs / f64 accumulate (positions f64)",
+        "data": "synthetic (seeded; no public dataset)",
+        "config": {"workload": desc + ", one full force evaluation per step", "n": n, "pairs_per_step": pairs_step,
+                   "parallelism": "one independent realisation per GPU" if ws > 1 else "1 GPU",
+                   "l2": "512 MB flush between steps", "precision": "mixed",
+                   "kernel_shape": shape_desc(r["shape"], args), "prep_ms": r["prep_ms"]},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(x_pin.nbytes),
+                "d2h_bytes_per_step": int(F_host.nbytes), "ms_per_step": e2e_t * 1e3,
+                "host_memory": "page-locked (steps_gpu_host_alloc)"},
+        "e2e_pageable": {"value": pairs_step / float(np.mean(e2e_pg)), "unit": UNIT,
+                         "ms_per_step": float(np.mean(e2e_pg)) * 1e3,
+                         "host_memory": "ordinary malloc'd numpy arrays, as the reference's driver passes x and F"},
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": f32_peak / 1e12, "unit": "TFLOP/s",
+                     "frac": r["frac"], "traffic": traffic_of(args.workload, n, timed_shape),
+                     "traffic_note": "DRAM bytes of one pair-kernel launch from an ncu capture of the timed shape "
+                                     "(null: no capture of this shape); compute-bound",
+                     "peak_kind": "FP32 FMA issue peak measured in this process (dependent-FMA-chain kernel); "
+                                  "MEASURED_PEAKS.json holds HBM and bf16-tensor figures only",
+                     "nominal_peak_at_sampled_clock": nominal, "sms": nsm,
+                     "frac_of_nominal": achieved / nominal if nominal else None,
+                     "flops_per_pair": flops, "kernel_ms": r["kernel_ms"]},
+        "fp64": r["fp64"],
+        "speedup_vs_fp64": r["speedup_vs_fp64"],
+        "accuracy_mixed_vs_fp64": r["accuracy"],
         "e2e_vs_resident_max_abs_diff": float(np.abs(F_host - Fmixed).max()),
-        "gpu_launches": int(launches),
+        "gpu_launches": r["launches"],
         "clocks": clk,
     }
-    return line, ps, p, host_table(table, eng)
+    eng.free_host_arrays()
+    return line, ps, p, host_table(table, eng), eng, (f32_peak, f64_peak)
 
 
-def run_batch(args, ws, rank, local, dist):
-    """Workload 4: 64 independent compactified R^3 realisations (seeds 0..63,
-    N_k log-uniform in [8192, 262144], R_max ~ U[200, 800]); one force
-    evaluation + 10 fixed-dt KDK steps, as one CUDA graph of persistent
-    work-list kernels, against 64 separate per-realisation launches."""
-    import steps_gb300 as S
-    from steps_gb300 import workloads as W
-
-    sets = W.r3_ensemble(64, scale=args.batch_scale)
+def batch_measure(eng, S, sets, steps, warmup, f32_peak, plain_steps=1):
+    """Workload 4: independent compactified R^3 realisations; one force
+    evaluation + 10 fixed-dt KDK steps as one CUDA graph of persistent
+    work-list kernels, against per-realisation plain launches."""
     nsteps, h = 10, 1e-3
     pairs = (nsteps + 1) * float(sum(float(s.n) ** 2 for s in sets))
-    eng = S.Engine(local)
-    eng.set_variant(1)
     p = S.params(S.R3)
     xs, ms, es = [s.x for s in sets], [s.m for s in sets], [s.eps for s in sets]
-    f32_peak, _ = eng.measure_peaks()
+    eng.set_variant(1)
 
     def timed(graph):
         eng.batch_set(xs, ms, es)
@@ -504,45 +593,175 @@ def run_batch(args, ws, rank, local, dist):
         eng.mark(3)
         return eng.elapsed_ms(2, 3)
 
-    for _ in range(max(1, args.warmup)):  # tunes the tile shape and captures the graph
+    for _ in range(max(1, warmup)):  # tunes the tile shape and captures the graph
         timed(True)
-    clocks = ClockSampler(local)
-    clocks.start()
     launches0 = eng.launch_count()
-    g_ms = [timed(True) for _ in range(args.steps)]
+    g_ms = [timed(True) for _ in range(steps)]
     launches = eng.launch_count() - launches0
-    plain_ms = [timed(False) for _ in range(max(1, args.steps // 2))]
-    clk = clocks.stop()
+    plain_ms = [timed(False) for _ in range(max(1, plain_steps))]
     x0, v0, F0 = eng.batch_get(0)
     # accuracy spot check: realisation 0's last forces against the FP64 kernel at the same positions
     eng.set_particles(sets[0].m, sets[0].eps)
     F64 = eng.forces(x0, p, S.FP64)
     rel = np.linalg.norm(F0 - F64, axis=1) / np.linalg.norm(F64, axis=1)
-    gt = allmax(dist, float(np.median(g_ms)))
+    gt = float(np.median(g_ms))
     pt = float(np.median(plain_ms))
-    value = ws * pairs / (gt * 1e-3)
+    value = pairs / (gt * 1e-3)
+    return {"value": value, "ms_per_step": gt, "pairs_per_step": pairs, "steps": steps, "launches": int(launches),
+            "total_particles": int(sum(s.n for s in sets)),
+            "plain_launches": {"pairs_per_s": pairs / (pt * 1e-3), "ms_per_step": pt,
+                               "what": "per-realisation force launches + KDK kernels"},
+            "speedup_graph_vs_plain": pt / gt, "frac": value * 20 / f32_peak,
+            "accuracy": {"p50": float(np.percentile(rel, 50)), "p99": float(np.percentile(rel, 99)),
+                         "max": float(rel.max()),
+                         "sample": f"realisation 0 (N={sets[0].n}) after the run, vs the FP64 kernel"}}
+
+
+def run_batch(args, ws, rank, local, dist):
+    import steps_gb300 as S
+    from steps_gb300 import workloads as W
+
+    sets = W.r3_ensemble(64, scale=args.batch_scale)
+    eng = S.Engine(local)
+    f32_peak, _ = eng.measure_peaks()
+    clocks = ClockSampler(local)
+    clocks.start()
+    r = batch_measure(eng, S, sets, args.steps, args.warmup, f32_peak, plain_steps=max(1, args.steps // 2))
+    clk = clocks.stop()
+    gt = allmax(dist, r["ms_per_step"])
+    value = ws * r["pairs_per_step"] / (gt * 1e-3)
     return {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": gt, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 pairs / f64 accumulate (positions f64)", "data": "synthetic (seeded; no public dataset)",
         "config": {"workload": f"batched ensemble: {len(sets)} R3 realisations, N_k log-uniform [8192, 262144] "
-                               f"(total {sum(s.n for s in sets)}), 1 force + {nsteps} KDK steps per step, one CUDA "
-                               "graph of persistent work-list kernels", "pairs_per_step": pairs,
+                               f"(total {r['total_particles']}), 1 force + 10 KDK steps per step, one CUDA "
+                               "graph of persistent work-list kernels", "pairs_per_step": r["pairs_per_step"],
                    "l2": "inputs re-uploaded before every step (outside the timed events)"},
-        "plain_launches": {"pairs_per_s": pairs / (pt * 1e-3), "ms_per_step": pt,
-                           "what": "64 separate per-realisation force launches + KDK kernels"},
-        "speedup_graph_vs_plain": pt / gt,
+        "plain_launches": r["plain_launches"],
+        "speedup_graph_vs_plain": r["speedup_graph_vs_plain"],
         "roofline": {"bound": "fp32", "achieved": value / ws * 20 / 1e12, "peak": f32_peak / 1e12,
-                     "unit": "TFLOP/s", "frac": value / ws * 20 / f32_peak, "traffic": None,
+                     "unit": "TFLOP/s", "frac": r["frac"], "traffic": None,
                      "peak_kind": "FP32 FMA issue peak measured in this process", "flops_per_pair": 20},
-        "accuracy_mixed_vs_fp64": {"p50": float(np.percentile(rel, 50)), "p99": float(np.percentile(rel, 99)),
-                                   "max": float(rel.max()),
-                                   "sample": f"realisation 0 (N={sets[0].n}) after the run, vs the FP64 kernel"},
-        "gpu_launches": int(launches),
+        "accuracy_mixed_vs_fp64": r["accuracy"],
+        "gpu_launches": r["launches"],
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
                 "note": "device-resident ensemble; see config"},
         "clocks": clk,
     }
+
+
+# The other workloads measured by the default run, with short samples.
+CONFIGS = [
+    ("cfg0", {"workload": "cfg0"}),
+    ("cfg2_images", {"workload": "cfg2"}),
+    ("cfg2_table_o0", {"workload": "cfg2", "s1_table": True, "order": 0, "n": 1 << 20}),
+    ("cfg2_table_o2", {"workload": "cfg2", "s1_table": True, "order": 2, "n": 1 << 20}),
+    ("cfg2_table_o4", {"workload": "cfg2", "s1_table": True, "order": 4, "n": 1 << 20}),
+    ("cfg3_o2", {"workload": "cfg3", "order": 2}),
+    ("cfg3_o4", {"workload": "cfg3", "order": 4}),
+    ("cfg3_o2_ng127", {"workload": "cfg3", "order": 2, "t3_level": 3}),
+]
+REF_GPU = [
+    ("r3", {"workload": "cfg1"}),
+    ("t3", {"workload": "cfg3", "order": 4}),
+    ("s1_images", {"workload": "cfg2"}),
+    ("s1_table_o0", {"workload": "cfg2", "s1_table": True, "order": 0, "n": 1 << 20}),
+    ("s1_table_o2", {"workload": "cfg2", "s1_table": True, "order": 2, "n": 1 << 20}),
+    ("s1_table_o4", {"workload": "cfg2", "s1_table": True, "order": 4, "n": 1 << 20}),
+]
+
+
+def config_args(args, over):
+    ns = argparse.Namespace(**vars(args))
+    ns.n, ns.order, ns.s1_table, ns.t3_level = 0, 2, False, 0
+    for k, v in over.items():
+        setattr(ns, k, v)
+    return ns
+
+
+def run_configs(args, eng, peaks, local):
+    """Every other workload, briefly: 1 warm-up + 3 timed evaluations (2 for the
+    slow ones), the FP64 kernel on 2048 i, a ~2 s CPU baseline sample."""
+    import steps_gb300 as S
+    from steps_gb300 import workloads as W
+
+    f32_peak, f64_peak = peaks
+    threads = os.cpu_count() or 1
+    out = {}
+    clocks = ClockSampler(local)
+    clocks.start()
+    t_all = time.perf_counter()
+    for name, over in CONFIGS:
+        t0 = time.perf_counter()
+        ca = config_args(args, over)
+        ps, p, flops, desc, table = workload(ca)
+        eng.set_variant(0)
+        setup_engine_workload(eng, ps, table)
+        slow = (ps.n * ps.n * flops) > 5e13
+        r = measure(eng, S, ps, p, flops, table, 2 if slow else 3, 1, 2048, f32_peak, f64_peak)
+        tab = host_table(table, eng)
+        rate, dt, pairs, ni = cpu_baseline(ps, p, 0, threads, tab, seconds=2.0)
+        out[name] = {"workload": desc, "value": r["value"], "unit": UNIT, "ms_per_step": float(np.mean(r["step_ms"])),
+                     "steps": len(r["step_ms"]), "kernel_ms": r["kernel_ms"], "prep_ms": r["prep_ms"],
+                     "kernel_pairs_per_s": r["kern_rate"], "kernel_shape": shape_desc(r["shape"], ca),
+                     "roofline": {"bound": "fp32", "frac": r["frac"], "achieved": r["achieved"],
+                                  "peak": f32_peak / 1e12, "unit": "TFLOP/s", "flops_per_pair": flops},
+                     "fp64": r["fp64"], "speedup_vs_fp64": r["speedup_vs_fp64"],
+                     "accuracy_mixed_vs_fp64": r["accuracy"],
+                     "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                                      "sample": f"{ni} i particles x all {ps.n} j ({dt:.1f} s)"},
+                     "wall_s": time.perf_counter() - t0}
+    t0 = time.perf_counter()
+    sets = W.r3_ensemble(64)
+    r = batch_measure(eng, S, sets, 2, 1, f32_peak)
+    out["cfg4"] = {"workload": f"batched ensemble: 64 R3 realisations, N_k log-uniform [8192, 262144] "
+                               f"(total {r['total_particles']}), 1 force + 10 KDK steps, one CUDA graph",
+                   "value": r["value"], "unit": UNIT, "ms_per_step": r["ms_per_step"], "steps": r["steps"],
+                   "roofline": {"bound": "fp32", "frac": r["frac"], "peak": f32_peak / 1e12, "flops_per_pair": 20},
+                   "plain_launches": r["plain_launches"], "speedup_graph_vs_plain": r["speedup_graph_vs_plain"],
+                   "accuracy_mixed_vs_fp64": r["accuracy"], "wall_s": time.perf_counter() - t0}
+    eng.set_variant(0)
+    clk = clocks.stop()
+    out["_clocks"] = clk
+    out["_wall_s"] = time.perf_counter() - t_all
+    return out
+
+
+def run_ref_gpu_block(args):
+    out = {}
+    t_all = time.perf_counter()
+    for name, over in REF_GPU:
+        ca = config_args(args, over)
+        ps, p, flops, desc, table = workload(ca)
+        r = ref_gpu_measure(ca, ps, p, flops, desc, table, 0.5, 2, 1)
+        if r is None:
+            return {"unavailable": "oracle/_ref/forces_cuda_*.cubin not built (needs the reference tree at build time)"}
+        out[name] = r
+    out["_wall_s"] = time.perf_counter() - t_all
+    return out
+
+
+def add_ratios(line):
+    """Our kernel's pair rate over the reference CUDA builds' on the same
+    workloads (kernel time against kernel time)."""
+    cf, rg = line.get("configs") or {}, line.get("ref_gpu") or {}
+    pairs = {"r3": None, "t3": "cfg3_o4", "s1_images": "cfg2_images", "s1_table_o0": "cfg2_table_o0",
+             "s1_table_o2": "cfg2_table_o2", "s1_table_o4": "cfg2_table_o4"}
+    for name, ours in pairs.items():
+        r = rg.get(name)
+        if not isinstance(r, dict) or "fp32_build" not in r:
+            continue
+        if ours is None:  # the headline workload
+            mixed = line["config"]["pairs_per_step"] / (line["roofline"]["kernel_ms"] * 1e-3)
+            f64 = line["fp64"]["pairs_per_s"]
+        else:
+            mixed = cf.get(ours, {}).get("kernel_pairs_per_s")
+            f64 = cf.get(ours, {}).get("fp64", {}).get("pairs_per_s")
+        if mixed:
+            r["mixed_over_ref_fp32"] = mixed / r["fp32_build"]["pairs_per_s"]
+        if f64:
+            r["fp64_over_ref_fp64"] = f64 / r["fp64_build"]["pairs_per_s"]
 
 
 def main():
@@ -562,13 +781,17 @@ def main():
         if dist is not None:
             dist.destroy_process_group()
         return
-    line, ps, p, tab = run_ours(args, ws, rank, local, dist)
+    line, ps, p, tab, eng, peaks = run_ours(args, ws, rank, local, dist)
     if rank == 0:
         threads = os.cpu_count() or 1
         rate, dt, pairs, ni = cpu_baseline(ps, p, args.cpu_sample, threads, tab, seconds=args.cpu_seconds)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                                 "build": "oracle port, -O3 -ffast-math (the reference's release flags)",
                                 "sample": f"{ni} i particles x all {ps.n} j ({dt:.1f} s of CPU work)"}
+        if ws == 1 and args.workload == "cfg1" and not args.no_configs and not args.n:
+            line["configs"] = run_configs(args, eng, peaks, local)
+            line["ref_gpu"] = run_ref_gpu_block(args)
+            add_ratios(line)
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

@@ -229,7 +229,8 @@ int steps_gpu_set_precision_guard(double ratio);
  * fastest; writes threads, ipt, variant to out[3]. Each candidate runs the
  * pair kernel on a strided sample of the range's i tiles (about 8192 i
  * particles against all j, at least two waves of work): one untimed launch,
- * then the median of three timed ones. Leaves no resident forces. */
+ * then the median of three timed ones; the three fastest are timed again on
+ * a sample four times larger. Leaves no resident forces. */
 int steps_gpu_autotune(const steps_params *p, int id_min, int id_max, int *out);
 
 /* Number of kernels this library has launched since init. */

@@ -13,6 +13,8 @@
 #include <atomic>
 #include <mutex>
 #include <string>
+#include <utility>
+#include <vector>
 
 #include "common.cuh"
 #include "context.cuh"
@@ -466,37 +468,50 @@ int steps_gpu_autotune(const steps_params *p, int id_min, int id_max, int *out)
         // Each candidate runs the pair kernel on a strided sample of the real
         // i tiles (about 8192 i particles, at least two waves of items; no
         // reduction): one untimed launch, then the median of three timed ones.
+        // The three fastest are timed again on a sample four times larger.
         struct SampleMode {
             Ctx &c;
-            explicit SampleMode(Ctx &cc) : c(cc) { c.tune_sample = true; }
+            explicit SampleMode(Ctx &cc) : c(cc) { c.tune_sample = 1; }
             ~SampleMode()
             {
-                c.tune_sample = false;
+                c.tune_sample = 0;
                 c.F_ni = 0;  // the sampled runs leave no usable forces
                 c.F_valid = false;
             }
         } mode(c);
+        auto time_shape = [&](const Shape &sh) {
+            c.shape = sh;
+            float t[4];
+            for (int r = 0; r < 4; r++) {
+                // the phase events bracket the pair kernel only
+                compute_forces(p, STEPS_MIXED, id_min, id_max, true);
+                STEPS_CUDA(cudaEventSynchronize(c.phase[2]));
+                STEPS_CUDA(cudaEventElapsedTime(&t[r], c.phase[1], c.phase[2]));
+            }
+            std::sort(t + 1, t + 4);
+            return t[2];
+        };
         compute_forces(p, STEPS_MIXED, id_min, id_max, false);  // orders the particles, loads modules
+        std::vector<std::pair<float, Shape>> timed;
         for (int v = 0; v < nvar; v++)
             for (auto &s : shapes) {
                 if (!shape_supported_for(kp, s[0], s[1])) continue;
                 if (v >= 1 && v <= 3 && !r3x2_kernel(s[0], s[1], false, r3x2_occ(v))) continue;
                 if (v == 4 && !r3x2_pipe_kernel(s[0], s[1])) continue;
-                c.shape.threads = s[0];
-                c.shape.ipt = s[1];
-                c.shape.jsplit = 0;
-                c.shape.variant = v;
-                float t[4];
-                for (int r = 0; r < 4; r++) {
-                    // the phase events bracket the pair kernel only
-                    compute_forces(p, STEPS_MIXED, id_min, id_max, true);
-                    STEPS_CUDA(cudaEventSynchronize(c.phase[2]));
-                    STEPS_CUDA(cudaEventElapsedTime(&t[r], c.phase[1], c.phase[2]));
-                }
-                std::sort(t + 1, t + 4);
-                const float ms = t[2];
-                if (ms < best) { best = ms; bestS = c.shape; }
+                Shape sh = keep;
+                sh.threads = s[0];
+                sh.ipt = s[1];
+                sh.jsplit = 0;
+                sh.variant = v;
+                timed.emplace_back(time_shape(sh), sh);
             }
+        std::stable_sort(timed.begin(), timed.end(), [](const std::pair<float, Shape> &a,
+                                                        const std::pair<float, Shape> &b) { return a.first < b.first; });
+        c.tune_sample = 4;
+        for (size_t k = 0; k < timed.size() && k < 3; k++) {
+            const float ms = time_shape(timed[k].second);
+            if (ms < best) { best = ms; bestS = timed[k].second; }
+        }
         c.shape = bestS;
         c.shape_fixed = true;
         if (out) { out[0] = bestS.threads; out[1] = bestS.ipt; out[2] = bestS.variant; }

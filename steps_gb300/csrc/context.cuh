@@ -51,7 +51,8 @@ struct Ctx {
 
     Shape shape;
     bool shape_fixed = false;
-    bool tune_sample = false;  // the autotuner's timing runs: a strided sample of i tiles, no reduction
+    int tune_sample = 0;  // the autotuner's timing runs: a strided sample of about tune_sample x 8192 i particles
+                          // (0: off), no reduction
     double last_pairs = 0.0;
 
     Batch *batch = nullptr;

@@ -526,9 +526,9 @@ void forces_mixed(const KParams &kp, const Tables &tb, const double *x, const do
     a.istride = 1;
     // The autotuner times a strided sample of the real i tiles (dense tiles,
     // the same j split): at least 8192 i particles and two waves of items.
-    const bool sample = c.tune_sample;
+    const bool sample = c.tune_sample > 0;
     if (sample) {
-        const int want = std::max(div_up(8192, T), div_up(2 * resident, S));
+        const int want = c.tune_sample * std::max(div_up(8192, T), div_up(2 * resident, S));
         if (want < nit) {
             a.istride = nit / want;
             a.nitems = want * S;
