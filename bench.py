@@ -432,7 +432,9 @@ def measure(eng, S, ps, p, flops, table, steps, warmup, fp64_sample, f32_peak, f
     library stream, L2 flushed between them), the FP64 kernel on an i sample
     and the mixed kernel's error against it. Positions must be resident."""
     n = ps.n
+    t_tune = time.perf_counter()
     shape = None if shape_fixed else eng.autotune(p)
+    t_tune = time.perf_counter() - t_tune
     for _ in range(warmup):
         eng.forces_resident(p, S.MIXED)
     eng.synchronize()
@@ -466,6 +468,7 @@ def measure(eng, S, ps, p, flops, table, steps, warmup, fp64_sample, f32_peak, f
     return {
         "step_ms": step_ms, "kernel_ms": kern_ms, "prep_ms": float(np.mean(prep_ms)), "kern_rate": kern_rate,
         "value": pairs_step * steps / (float(sum(step_ms)) * 1e-3), "shape": shape, "launches": int(launches),
+        "autotune_s": None if shape_fixed else t_tune,
         "achieved": achieved, "frac": achieved / (f32_peak / 1e12), "Fmixed": Fmixed,
         "fp64": {"pairs_per_s": f64_rate, "kernel_ms": f64_ms, "sample_i": fs,
                  "frac_of_fp64_peak": f64_rate * flops / f64_peak, "fp64_peak_tflops": f64_peak / 1e12},
@@ -549,7 +552,8 @@ def run_ours(args, ws, rank, local, dist):
         "config": {"workload": desc + ", one full force evaluation per step", "n": n, "pairs_per_step": pairs_step,
                    "parallelism": "one independent realisation per GPU" if ws > 1 else "1 GPU",
                    "l2": "512 MB flush between steps", "precision": "mixed",
-                   "kernel_shape": shape_desc(r["shape"], args), "prep_ms": r["prep_ms"]},
+                   "kernel_shape": shape_desc(r["shape"], args), "prep_ms": r["prep_ms"],
+                   "autotune_s": r["autotune_s"]},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(x_pin.nbytes),
                 "d2h_bytes_per_step": int(F_host.nbytes), "ms_per_step": e2e_t * 1e3,
                 "host_memory": "page-locked (steps_gpu_host_alloc)"},
@@ -705,6 +709,7 @@ def run_configs(args, eng, peaks, local):
         out[name] = {"workload": desc, "value": r["value"], "unit": UNIT, "ms_per_step": float(np.mean(r["step_ms"])),
                      "steps": len(r["step_ms"]), "kernel_ms": r["kernel_ms"], "prep_ms": r["prep_ms"],
                      "kernel_pairs_per_s": r["kern_rate"], "kernel_shape": shape_desc(r["shape"], ca),
+                     "autotune_s": r["autotune_s"],
                      "roofline": {"bound": "fp32", "frac": r["frac"], "achieved": r["achieved"],
                                   "peak": f32_peak / 1e12, "unit": "TFLOP/s", "flops_per_pair": flops},
                      "fp64": r["fp64"], "speedup_vs_fp64": r["speedup_vs_fp64"],

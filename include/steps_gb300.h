@@ -226,11 +226,10 @@ int steps_gpu_set_precision_guard(double ratio);
 
 /* Times every supported mixed-precision shape on the resident particles for
  * the given topology -- for R^3 with each pair-loop variant -- and keeps the
- * fastest; writes threads, ipt, variant to out[3]. Each candidate runs the
- * pair kernel on a strided sample of the range's i tiles (about 8192 i
- * particles against all j, at least two waves of work): one untimed launch,
- * then the median of three timed ones; the three fastest are timed again on
- * a sample four times larger. Leaves no resident forces. */
+ * fastest; writes threads, ipt, variant to out[3]. Each candidate is first
+ * timed on a strided sample of the range's i tiles against all j, 24 waves
+ * of work (after one untimed launch); the three best are timed again on 96
+ * waves (or the whole range when it is smaller). Leaves no resident forces. */
 int steps_gpu_autotune(const steps_params *p, int id_min, int id_max, int *out);
 
 /* Number of kernels this library has launched since init. */

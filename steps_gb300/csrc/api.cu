@@ -460,39 +460,41 @@ int steps_gpu_autotune(const steps_params *p, int id_min, int id_max, int *out)
         Ctx &c = g_ctx;
         static const int shapes[][2] = {{64, 1}, {64, 2}, {64, 4}, {128, 1}, {128, 2}, {128, 4}, {256, 1}, {256, 2}};
         Shape keep = c.shape;
-        float best = 1e30f;
         Shape bestS = keep;
         KParams kp = derive_params(p);
         // R^3: the scalar and packed pair loops as well.
         const int nvar = kp.topology == STEPS_R3 ? R3_VARIANTS : 1;
-        // Each candidate runs the pair kernel on a strided sample of the real
-        // i tiles (about 8192 i particles, at least two waves of items; no
-        // reduction): one untimed launch, then the median of three timed ones.
-        // The three fastest are timed again on a sample four times larger.
+        // Stage 1: each candidate is scored by its time per pair on a strided
+        // sample of the real i tiles, 24 waves of items (one untimed launch,
+        // one timed; the whole range if it is smaller). Fewer waves misrank
+        // the candidates: the launch ramp and the last wave weigh in.
+        // Stage 2: the three best are timed on 96 waves (or the whole range).
         struct SampleMode {
             Ctx &c;
-            explicit SampleMode(Ctx &cc) : c(cc) { c.tune_sample = 1; }
+            explicit SampleMode(Ctx &cc) : c(cc) {}
             ~SampleMode()
             {
                 c.tune_sample = 0;
-                c.F_ni = 0;  // the sampled runs leave no usable forces
+                c.F_ni = 0;  // the timing runs leave no usable forces
                 c.F_valid = false;
             }
         } mode(c);
-        auto time_shape = [&](const Shape &sh) {
+        // time per pair of one timed launch at a sample size (after `warm` untimed ones)
+        auto score = [&](const Shape &sh, int waves, int warm) {
             c.shape = sh;
-            float t[4];
-            for (int r = 0; r < 4; r++) {
+            c.tune_sample = waves;
+            float ms = 0.0f;
+            for (int r = 0; r <= warm; r++) {
                 // the phase events bracket the pair kernel only
                 compute_forces(p, STEPS_MIXED, id_min, id_max, true);
                 STEPS_CUDA(cudaEventSynchronize(c.phase[2]));
-                STEPS_CUDA(cudaEventElapsedTime(&t[r], c.phase[1], c.phase[2]));
+                STEPS_CUDA(cudaEventElapsedTime(&ms, c.phase[1], c.phase[2]));
             }
-            std::sort(t + 1, t + 4);
-            return t[2];
+            return (double)ms / c.last_pairs;
         };
+        c.tune_sample = 1;
         compute_forces(p, STEPS_MIXED, id_min, id_max, false);  // orders the particles, loads modules
-        std::vector<std::pair<float, Shape>> timed;
+        std::vector<std::pair<double, Shape>> scored;
         for (int v = 0; v < nvar; v++)
             for (auto &s : shapes) {
                 if (!shape_supported_for(kp, s[0], s[1])) continue;
@@ -503,14 +505,14 @@ int steps_gpu_autotune(const steps_params *p, int id_min, int id_max, int *out)
                 sh.ipt = s[1];
                 sh.jsplit = 0;
                 sh.variant = v;
-                timed.emplace_back(time_shape(sh), sh);
+                scored.emplace_back(score(sh, 24, 1), sh);
             }
-        std::stable_sort(timed.begin(), timed.end(), [](const std::pair<float, Shape> &a,
-                                                        const std::pair<float, Shape> &b) { return a.first < b.first; });
-        c.tune_sample = 4;
-        for (size_t k = 0; k < timed.size() && k < 3; k++) {
-            const float ms = time_shape(timed[k].second);
-            if (ms < best) { best = ms; bestS = timed[k].second; }
+        std::stable_sort(scored.begin(), scored.end(), [](const std::pair<double, Shape> &a,
+                                                          const std::pair<double, Shape> &b) { return a.first < b.first; });
+        double best = 1e300;
+        for (size_t k = 0; k < scored.size() && k < 3; k++) {
+            const double sc = score(scored[k].second, 96, 0);
+            if (sc < best) { best = sc; bestS = scored[k].second; }
         }
         c.shape = bestS;
         c.shape_fixed = true;

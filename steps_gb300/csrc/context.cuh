@@ -51,8 +51,9 @@ struct Ctx {
 
     Shape shape;
     bool shape_fixed = false;
-    int tune_sample = 0;  // the autotuner's timing runs: a strided sample of about tune_sample x 8192 i particles
-                          // (0: off), no reduction
+    int tune_sample = 0;  // the autotuner's timing runs: tune_sample waves of items over a strided sample of
+                          // i tiles (0: off), no reduction
+    bool tune_sampled = false;  // the last timing run was cut to a sample (else it covered the whole range)
     double last_pairs = 0.0;
 
     Batch *batch = nullptr;

@@ -485,21 +485,16 @@ void forces_mixed(const KParams &kp, const Tables &tb, const double *x, const do
     const int nit = ti.ntiles, njt = c.tj.ntiles;
     int S = c.shape.jsplit;
     if (S <= 0) {
-        double best = 1e30;
-        S = 1;
-        // The FP64 chunk partials (S x N_i x 24 B) stay within 4 GiB.
+        // Items of at most 64 and at least 4 j tiles, aiming at 16 or more
+        // waves of items over the persistent grid: long items balance badly
+        // (near-field tile pairs make their lengths uneven), very short ones
+        // pay the per-item set-up. The FP64 chunk partials (S x N_i x 24 B)
+        // stay within 4 GiB.
         const long long smax = std::max(1LL, (4LL << 30) / ((long long)nit * T * 24));
-        for (int s = 1; s <= 64 && s <= njt && s <= smax; s++) {
-            int tpc = div_up(njt, s);
-            int sc = div_up(njt, tpc);
-            long long items = (long long)nit * sc;
-            long long waves = (items + resident - 1) / resident;
-            // cost ~ waves * item length, plus a small per-item overhead: finer
-            // items balance better than this model says (a per-item set-up of
-            // half a j tile in the model measured 3-6 % slower)
-            double cost = (double)waves * tpc + 0.02 * (double)items / resident;
-            if (cost < best - 1e-9) { best = cost; S = s; }
-        }
+        const long long pairs = (long long)nit * njt;
+        const long long tpc = std::min(64LL, std::max(4LL, pairs / (16LL * resident)));
+        S = (int)std::min<long long>(smax, (njt + tpc - 1) / tpc);
+        if (S < 1) S = 1;
     }
     if (S > njt) S = njt;
     const int tpc = div_up(njt, S);
@@ -525,13 +520,16 @@ void forces_mixed(const KParams &kp, const Tables &tb, const double *x, const do
     a.nitems = nit * S;
     a.istride = 1;
     // The autotuner times a strided sample of the real i tiles (dense tiles,
-    // the same j split): at least 8192 i particles and two waves of items.
+    // the same j split): tune_sample waves of items.
     const bool sample = c.tune_sample > 0;
+    c.tune_sampled = false;
     if (sample) {
-        const int want = c.tune_sample * std::max(div_up(8192, T), div_up(2 * resident, S));
-        if (want < nit) {
-            a.istride = nit / want;
-            a.nitems = want * S;
+        const long long want = (long long)c.tune_sample * resident;
+        if (want < (long long)a.nitems) {
+            const int tiles = (int)((want + S - 1) / S);
+            a.istride = std::max(1, nit / tiles);
+            a.nitems = (int)want;  // the last sampled tile may run only some of its chunks
+            c.tune_sampled = true;
         }
     }
     a.counter = c.counter.ensure<unsigned>(4);
@@ -585,8 +583,7 @@ void forces_mixed(const KParams &kp, const Tables &tb, const double *x, const do
     }
     STEPS_CUDA(cudaEventRecord(c.phase[3], st));
     c.phase_valid = true;
-    c.last_pairs = (double)(a.nitems / S) * T * (double)n;
-    if (!sample) c.last_pairs = (double)ni * (double)n;
+    c.last_pairs = c.tune_sampled ? (double)a.nitems * T * ((double)tpc * T) : (double)ni * (double)n;
 }
 
 }  // namespace steps
