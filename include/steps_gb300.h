@@ -132,9 +132,42 @@ int steps_gpu_set_table_s1r2(int nrho, int nz, const double *table);
 int steps_gpu_build_table_s1r2(int nrho, int nz, double rho_max, double lz, double alpha, int nmax, int mmax);
 int steps_gpu_get_table_s1r2(double *out);
 
+/* Loads a T^3 table file written by the reference's driver
+ * (save_t3_ewald_lookup_table, StePS/src/inputoutput.cc:1792: dataset
+ * /t3_ewald/T3_EWALD_FORCE_TABLE of (Ng, Ng, Ng, 3) doubles, or floats from a
+ * single-precision build) and makes it the current table, as
+ * steps_gpu_set_table_t3 does; *ngrid_out (may be NULL) receives Ng. Reads the
+ * file layout the HDF5 library writes with default properties (no HDF5
+ * installation needed); other layouts return STEPS_E_ARG with the reason. */
+int steps_gpu_load_table_t3_hdf5(const char *path, int *ngrid_out);
+
+/* The same for an S1xR2 table file (save_s1r2_ewald_lookup_table,
+ * StePS/src/inputoutput.cc:2102: /s1r2_ewald/S1R2_EWALD_FORCE_TABLE of
+ * (Nrho, Nz, 2)). */
+int steps_gpu_load_table_s1r2_hdf5(const char *path, int *nrho_out, int *nz_out);
+
+/* The reader behind the two loaders, for any dataset of such a file (no GPU
+ * needed): `dataset` is an absolute path ("/group/name"); integer and
+ * floating-point elements are converted to double. Writes *rank, dims[rank]
+ * (up to 32) and *count (any may be NULL); copies the elements into out when
+ * out is non-NULL and capacity >= count. */
+int steps_h5_read_f64(const char *path, const char *dataset, double *out, long long capacity, long long *count,
+                      int *rank, long long *dims);
+
 /* Cylindrical background multiplier table RADIAL_FORCE_TABLE[size]
  * (StePS/src/utils.cc:162-228), used by S1xR2 comoving runs. */
 int steps_gpu_set_radial_table(int size, const double *table);
+
+/* Builds that table on the GPU in FP64 -- get_cylindrical_force_table
+ * (StePS/src/utils.cc:162-228): the pull at r_i = rsim i / (size - 1) of a
+ * finite cylinder of half length lz by the trapezoid rule over `accuracy`
+ * intervals (RADIAL_FORCE_TABLE_SIZE, RADIAL_FORCE_ACCURACY; the reference's
+ * driver passes lz = L/2 at IS_PERIODIC = 1 and L (IS_PERIODIC + 0.6) above,
+ * StePS/src/main.cc:905-917) -- and keeps it as the radial table. */
+int steps_gpu_build_radial_table(int size, double rsim, double lz, int accuracy);
+
+/* Copies the current radial table (size doubles) to the host. */
+int steps_gpu_get_radial_table(double *out);
 
 /* ---- force evaluation --------------------------------------------------- */
 

@@ -75,6 +75,26 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     return lib
 
 
+def h5_read(path, dataset):
+    """A dataset of an HDF5 file in the layout the HDF5 library writes by
+    default (the reference's table files), as float64, with its shape;
+    through steps_h5_read_f64 (no GPU needed)."""
+    lib = load_library()
+    fn = lib.steps_h5_read_f64
+    fn.argtypes = [C.c_char_p, C.c_char_p, C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong), C.POINTER(C.c_int),
+                   C.POINTER(C.c_longlong)]
+    cnt, rank, dims = C.c_longlong(0), C.c_int(0), (C.c_longlong * 32)()
+    args = (os.fsencode(path), dataset.encode())
+    rc = fn(*args, None, 0, C.byref(cnt), C.byref(rank), dims)
+    if rc != STEPS_OK:
+        raise StepsError(rc, lib.steps_gpu_error_string().decode())
+    out = np.empty(cnt.value)
+    rc = fn(*args, out.ctypes.data, cnt.value, None, None, None)
+    if rc != STEPS_OK:
+        raise StepsError(rc, lib.steps_gpu_error_string().decode())
+    return out.reshape([dims[k] for k in range(rank.value)])
+
+
 def _d(a: np.ndarray):
     return a.ctypes.data_as(_dp)
 
@@ -183,9 +203,33 @@ class Engine:
         self._check(self.lib.steps_gpu_get_table_s1r2(_d(out)))
         return out
 
+    def load_table_t3_hdf5(self, path):
+        ng = C.c_int(0)
+        self.lib.steps_gpu_load_table_t3_hdf5.argtypes = [C.c_char_p, C.POINTER(C.c_int)]
+        self._check(self.lib.steps_gpu_load_table_t3_hdf5(os.fsencode(path), C.byref(ng)))
+        self.t3_ng = ng.value
+        return ng.value
+
+    def load_table_s1r2_hdf5(self, path):
+        nrho, nz = C.c_int(0), C.c_int(0)
+        self.lib.steps_gpu_load_table_s1r2_hdf5.argtypes = [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        self._check(self.lib.steps_gpu_load_table_s1r2_hdf5(os.fsencode(path), C.byref(nrho), C.byref(nz)))
+        self.s1r2_shape = (nrho.value, nz.value)
+        return nrho.value, nz.value
+
     def set_radial_table(self, tab):
         tab = np.ascontiguousarray(tab, dtype=np.float64)
         self._check(self.lib.steps_gpu_set_radial_table(int(tab.size), _d(tab)))
+
+    def build_radial_table(self, size, rsim, lz, accuracy):
+        self.lib.steps_gpu_build_radial_table.argtypes = [C.c_int, C.c_double, C.c_double, C.c_int]
+        self._check(self.lib.steps_gpu_build_radial_table(int(size), float(rsim), float(lz), int(accuracy)))
+        self.radial_size = int(size)
+
+    def get_radial_table(self, size=None):
+        out = np.empty(size or self.radial_size)
+        self._check(self.lib.steps_gpu_get_radial_table(_d(out)))
+        return out
 
     # batched ensembles
     def batch_set(self, xs, ms, epss):

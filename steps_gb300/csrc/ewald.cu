@@ -269,6 +269,73 @@ __global__ void k_s1r2_table(int nrho, int nz, double rho_max, double lz, double
     tab[2 * (size_t)id + 1] = Fz - Fzn;
 }
 
+// ---- cylindrical radial background multiplier (finite Ewald cylinder) ----
+//
+// RADIAL_FORCE_TABLE[i] for S1xR2 comoving runs: the radial pull of the matter
+// outside the simulation cylinder relative to an infinite cylinder, at
+// r_i = R i / (size - 1), by the trapezoid rule over `accuracy` intervals of
+// Y in [0, R] (StePS/src/utils.cc:162-228). The integrand is the reference's
+// closed form, evaluated with the same operation order (squares as products,
+// square roots, no contraction); the trapezoid terms are summed per thread
+// in order and the threads' sums in a fixed tree, so the table is
+// deterministic and within rounding of the reference's sequential sum.
+constexpr double RADIAL_PI = 3.14159265358979323846264338327950288419716939937510;
+constexpr int RADIAL_THREADS = 128;
+
+__device__ double radial_integrand(double R, double lz, double a, double Y, bool at_edge)
+{
+    const double s = sqrt(R * R - Y * Y);
+    if (at_edge)  // a = R (utils.cc:186-191)
+        return -2 * log((sqrt(lz * lz + 2 * (R * R) + 2 * R * s) + lz) / (sqrt(lz * lz + 2 * (R * R) - 2 * R * s) + lz));
+    const double f1 = -2 * log((sqrt(lz * lz + R * R + a * a + 2 * a * s) + lz) / (sqrt(lz * lz + R * R + a * a - 2 * a * s) + lz));
+    const double f2 = log((R * R + a * a + 2 * a * s) / (R * R + a * a - 2 * a * s));
+    return f1 + f2;
+}
+
+__global__ void __launch_bounds__(RADIAL_THREADS) k_radial_table(double R, double lz, int size, int accuracy,
+                                                                 double *__restrict__ out)
+{
+    __shared__ double part[RADIAL_THREADS];
+    const int i = blockIdx.x + 1;  // entry 0 is interpolated afterwards
+    const double step = R / (double)accuracy;
+    double a = i == size - 1 ? R : R / (double)(size - 1) * i;
+    const bool edge = a >= R;
+    if (edge) a = R;
+    // thread t sums the contiguous terms j in [j0, j1) in order
+    const int per = (accuracy + RADIAL_THREADS - 1) / RADIAL_THREADS;
+    const int j0 = 1 + threadIdx.x * per, j1 = min(accuracy + 1, j0 + per);
+    double sum = 0.0;
+    for (int j = j0; j < j1; j++) {
+        const double ip = radial_integrand(R, lz, a, (j - 1) * step, edge);
+        const double in = radial_integrand(R, lz, a, j * step, edge);
+        sum += step * (ip + in) * 0.5;
+    }
+    part[threadIdx.x] = sum;
+    __syncthreads();
+    for (int o = RADIAL_THREADS / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) part[threadIdx.x] += part[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double total = part[0];
+        out[i] = edge ? 2 * (total + RADIAL_PI * R) / (2 * RADIAL_PI * R) : 2 * total / (2 * RADIAL_PI * a);
+    }
+}
+
+// Entry 0 by the reference's linear extrapolation from entries 1 and 2, taken
+// at r = 2R/size and 4R/size (utils.cc:224-227, linear_interpolation utils.cc:24-37).
+__global__ void k_radial_table0(double R, int size, double *out)
+{
+    if (size < 3) {
+        out[0] = 0.0;
+        return;
+    }
+    const double x1 = 2 * R / (double)size, x2 = 4 * R / (double)size;
+    const double A = (out[2] - out[1]) / (x2 - x1);
+    const double B = out[1] - A * x1;
+    out[0] = A * 0.0 + B;
+}
+
 }  // namespace
 
 }  // namespace steps
@@ -276,6 +343,47 @@ __global__ void k_s1r2_table(int nrho, int nz, double rho_max, double lz, double
 using namespace steps;
 
 extern "C" {
+
+int steps_gpu_build_radial_table(int size, double rsim, double lz, int accuracy)
+{
+    struct A {
+        int size;
+        double rsim, lz;
+        int accuracy;
+    } a{size, rsim, lz, accuracy};
+    return run_guarded(
+        [](void *p) {
+            A &a = *static_cast<A *>(p);
+            require_init();
+            Ctx &c = ctx();
+            if (a.size < 2 || a.size > (1 << 24) || a.accuracy < 1 || a.accuracy > (1 << 24) || !(a.rsim > 0) ||
+                !(a.lz > 0))
+                fail(STEPS_E_ARG, "build_radial_table: size >= 2, accuracy >= 1, rsim > 0 and lz > 0 required");
+            double *tab = c.radial.ensure<double>(a.size);
+            k_radial_table<<<a.size - 1, RADIAL_THREADS, 0, c.stream>>>(a.rsim, a.lz, a.size, a.accuracy, tab);
+            note_launch("k_radial_table");
+            k_radial_table0<<<1, 1, 0, c.stream>>>(a.rsim, a.size, tab);
+            note_launch("k_radial_table0");
+            STEPS_CUDA(cudaStreamSynchronize(c.stream));
+            c.radial_size = a.size;
+        },
+        &a);
+}
+
+int steps_gpu_get_radial_table(double *out)
+{
+    return run_guarded(
+        [](void *p) {
+            require_init();
+            Ctx &c = ctx();
+            if (!p) fail(STEPS_E_ARG, "out is NULL");
+            if (c.radial_size <= 0) fail(STEPS_E_STATE, "no radial table");
+            STEPS_CUDA(cudaMemcpyAsync(p, c.radial.as<double>(), sizeof(double) * c.radial_size,
+                                       cudaMemcpyDeviceToHost, c.stream));
+            STEPS_CUDA(cudaStreamSynchronize(c.stream));
+        },
+        out);
+}
 
 int steps_gpu_build_table_t3(int ngrid, double L, double alpha, double rel_cut, double rec_cut, double real_radius,
                              double rec_radius)

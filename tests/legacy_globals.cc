@@ -4,6 +4,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <vector>
+
 #ifdef USE_SINGLE_PRECISION
 typedef float REAL;
 #else
@@ -81,16 +83,22 @@ void h_softening(double radius, double m_min, int cosmology, double *beta_out, d
     *beta_out = beta;
     *rho_out = rho_part;
 }
+// Positions and forces pass through REAL arrays, as the driver holds them
+// (float in a USE_SINGLE_PRECISION build, StePS/src/global_variables.h:26-32).
 int h_forces(double *x, double *F, int id_min, int id_max)
 {
     ForceError = false;
+    const int ni = id_max - id_min + 1;
+    std::vector<REAL> xr(x, x + 3 * (size_t)N), Fr(3 * (size_t)(ni > 0 ? ni : 1));
+    for (int k = 0; k < 3 * (ni > 0 ? ni : 1); k++) Fr[k] = (REAL)F[k];
 #if defined(PERIODIC)
-    forces_periodic(x, F, id_min, id_max);
+    forces_periodic(xr.data(), Fr.data(), id_min, id_max);
 #elif defined(PERIODIC_Z)
-    forces_periodic_z(x, F, id_min, id_max);
+    forces_periodic_z(xr.data(), Fr.data(), id_min, id_max);
 #else
-    forces(x, F, id_min, id_max);
+    forces(xr.data(), Fr.data(), id_min, id_max);
 #endif
+    for (int k = 0; k < 3 * (ni > 0 ? ni : 0); k++) F[k] = Fr[k];
     return ForceError ? 1 : 0;
 }
 }

@@ -10,14 +10,20 @@ import subprocess
 import numpy as np
 import pytest
 
+import pyoracle as O
 import steps_gb300 as S
-from helpers import err_stats, golden, rel_err
+from helpers import err_stats, golden, port_params, rel_err
+from steps_gb300 import workloads as W
 
 pytestmark = pytest.mark.gpu
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 FLAGS = {"r3": [], "t3": ["-DPERIODIC", "-DEWALD_INTERPOLATION_ORDER=4"],
-         "s1nl": ["-DPERIODIC_Z", "-DPERIODIC_Z_NOLOOKUP"], "s1tab": ["-DPERIODIC_Z", "-DEWALD_INTERPOLATION_ORDER=2"]}
+         "s1nl": ["-DPERIODIC_Z", "-DPERIODIC_Z_NOLOOKUP"], "s1tab": ["-DPERIODIC_Z", "-DEWALD_INTERPOLATION_ORDER=2"],
+         # REAL = float builds (USE_SINGLE_PRECISION, StePS/src/global_variables.h:26-32)
+         "r3sp": ["-DUSE_SINGLE_PRECISION"],
+         "t3o2sp": ["-DPERIODIC", "-DEWALD_INTERPOLATION_ORDER=2", "-DUSE_SINGLE_PRECISION"],
+         "s1nlsp": ["-DPERIODIC_Z", "-DPERIODIC_Z_NOLOOKUP", "-DUSE_SINGLE_PRECISION"]}
 _dp = C.POINTER(C.c_double)
 
 
@@ -116,3 +122,83 @@ def test_forces_periodic_z(tmp_path_factory, engine):
     h.h_precision(S.FP64)
     rc, F = run(h, g["x"], 2048)
     assert rc == 0 and rel_err(F, g["F"]).max() < 1e-12
+
+
+def f32(a):
+    """What a REAL = float driver holds of a double array."""
+    return np.asarray(a, dtype=np.float32).astype(np.float64)
+
+
+def _single_precision_case(h, engine, port_sys, port, x, m, eps, p, F32_ref, lo, hi):
+    """The shim in a REAL = float build. The driver hands it float positions,
+    masses and softening, so its results are checked against this library's
+    kernels on those float inputs (the shim converts them to double exactly):
+    FP64 mode equals the FP64 kernel, and mixed mode the mixed kernel of the
+    same shape (the shim's autotuning is off), each to one FP32 rounding of
+    the output; the FP64 kernel on them equals the oracle (1e-12); and mixed
+    mode keeps p99 <= 1e-5 against that FP64 answer. The reference's own FP32
+    build, on the same float inputs, is at the same error level (its
+    statistics are in the assertion message); against the FP64 answer on the
+    unrounded inputs the mixed kernel is compared with it in
+    test_gpu_fp32_floor.py."""
+    n = x.shape[0]
+    engine.set_particles(f32(m), f32(eps))
+    truth = engine.forces(f32(x), p, S.FP64)
+    port_truth = port.forces(port_sys, f32(x), lo, hi)
+    assert rel_err(truth[lo:hi + 1], port_truth).max() < 1e-12
+    engine.set_tuning(128, 2, 0)
+    engine.set_variant(0)
+    mixed = engine.forces(f32(x), p, S.MIXED)
+    h.h_precision(S.FP64)
+    rc, F = run(h, x, 0)
+    assert rc == 0 and F.shape[0] == n
+    assert rel_err(F, truth).max() < 2e-7  # one FP32 rounding of each component
+    h.h_precision(S.MIXED)
+    rc, F = run(h, x, 0)
+    assert rc == 0
+    assert rel_err(F, mixed).max() < 2e-7
+    ours, theirs = err_stats(F[lo:hi + 1], truth[lo:hi + 1]), err_stats(F32_ref, port_truth)
+    assert ours["p99"] < 1e-5, ("mixed", ours, "reference FP32 build", theirs)
+
+
+@pytest.fixture
+def no_shim_autotune(monkeypatch):
+    monkeypatch.setenv("STEPS_GB300_AUTOTUNE", "0")
+
+
+def test_single_precision_build_r3(tmp_path_factory, engine, port, no_shim_autotune):
+    f = golden("ref_fp32")
+    ps = W.r3_compactified(int(f["r3_n"]), float(f["r3_rmax"]), seed=int(f["r3_seed"]))
+    lo, hi = (int(v) for v in f["r3_sub"])
+    h = harness(tmp_path_factory, "r3sp")
+    h.h_set(ps.n, np.ascontiguousarray(ps.m).ctypes.data_as(_dp), np.ascontiguousarray(ps.eps).ctypes.data_as(_dp),
+            0, 0.0, 0.0, 0, 0, 0.0)
+    s = port.system(0, f32(ps.m), f32(ps.eps), port_params(O))
+    _single_precision_case(h, engine, s, port, ps.x, ps.m, ps.eps, S.params(S.R3), f["r3_F32"], lo, hi)
+
+
+def test_single_precision_build_t3(tmp_path_factory, engine, port, no_shim_autotune):
+    g, f = golden("t3_o2"), golden("ref_fp32")
+    ng, L = int(g["ngrid"]), float(g["L"])
+    Lf, rf = float(np.float32(L)), float(np.float32(L / 2))
+    h = harness(tmp_path_factory, "t3o2sp")
+    set_particles(h, g, 2, L, L / 2)
+    t = np.ascontiguousarray(g["table"])
+    h.h_table(t.ctypes.data_as(_dp), ng, 0)
+    engine.set_table_t3(f32(g["table"]), ng)  # what the float build uploads
+    p = S.params(S.T3, is_periodic=2, L=Lf, rsim=rf, ewald_order=2)
+    s = port.system(1, f32(g["m"]), f32(g["eps"]), port_params(O, is_periodic=2, L=Lf, rsim=rf),
+                    table=f32(g["table"]), ngrid=ng, order=2)
+    n = g["x"].shape[0]
+    _single_precision_case(h, engine, s, port, g["x"], g["m"], g["eps"], p, f["t3o2_F32"], 0, n - 1)
+
+
+def test_single_precision_build_s1r2(tmp_path_factory, engine, port, no_shim_autotune):
+    g, f = golden("s1r2_images"), golden("ref_fp32")
+    Lf, rf = float(np.float32(float(g["L"]))), float(np.float32(float(g["rsim"])))
+    h = harness(tmp_path_factory, "s1nlsp")
+    set_particles(h, g, 2, float(g["L"]), float(g["rsim"]))
+    p = S.params(S.S1R2, is_periodic=2, L=Lf, rsim=rf, s1r2_images=1)
+    s = port.system(3, f32(g["m"]), f32(g["eps"]), port_params(O, is_periodic=2, L=Lf, rsim=rf))
+    n = g["x"].shape[0]
+    _single_precision_case(h, engine, s, port, g["x"], g["m"], g["eps"], p, f["s1r2_is2_F32"], 0, n - 1)

@@ -1,13 +1,14 @@
 """S1xR2 and T^3 forces and Ewald tables on the GPU through the C-ABI,
 against the reference's golden vectors and the plain-C oracle."""
 import math
+import os
 
 import numpy as np
 import pyoracle as O
 import pytest
 
 import steps_gb300 as S
-from helpers import err_stats, golden, port_params, rel_err
+from helpers import GOLDEN, err_stats, golden, port_params, rel_err
 from steps_gb300 import workloads as W
 
 pytestmark = pytest.mark.gpu
@@ -408,3 +409,49 @@ def test_periodic_edge_sizes(engine, port, mode, n):
         check(Fl, Fo[lo:lo + 1], big[lo:lo + 1], FP64_TOL, 1e-12)
         Fl = engine.forces(x, p, S.MIXED, lo, lo)
         check(Fl, Fo[lo:lo + 1], big[lo:lo + 1], 1e-4, 1e-6)
+
+
+def test_radial_table_builder(engine, port):
+    """The GPU builder of the cylindrical background multiplier
+    (get_cylindrical_force_table, StePS/src/utils.cc:162-228) against the
+    reference build's own table in the golden set, then used in a comoving
+    S1xR2 evaluation against the reference's forces; and at the reference's
+    default size and accuracy (1000 x 1000) against the oracle."""
+    g = golden("s1r2_images")
+    L, rsim = float(g["L"]), float(g["rsim"])
+    ewald_cut = 3 - 0.4  # IS_PERIODIC = 2 (StePS/src/main.cc:1270-1271)
+    engine.build_radial_table(200, rsim, L * ewald_cut, 400)
+    tab = engine.get_radial_table(200)
+    np.testing.assert_allclose(tab, g["radial"], rtol=1e-12, atol=1e-14)
+    engine.set_particles(g["m"], g["eps"])
+    p = s1_params(g, 2, cosmology=1, comoving=1, mius=float(g["mius"]))
+    assert rel_err(engine.forces(g["x"], p, S.FP64), g["F_comoving"]).max() < FP64_TOL
+    for lz in (0.5 * L, 5.6 * L):
+        engine.build_radial_table(1000, rsim, lz, 1000)
+        np.testing.assert_allclose(engine.get_radial_table(1000), port.cyl_table(rsim, lz, 1000, 1000), rtol=1e-12,
+                                   atol=1e-14)
+
+
+def test_load_tables_from_hdf5(engine):
+    """Table files in the reference's HDF5 layout (StePS/src/inputoutput.cc:
+    1792, 2102; tests/golden/make_h5_tables.py) loaded into the GPU context:
+    the tables arrive bit for bit and give the reference's FP64 forces."""
+    g = golden("t3_o2")
+    L = float(g["L"])
+    ng = engine.load_table_t3_hdf5(os.path.join(GOLDEN, "t3_table_ng17.h5"))
+    assert ng == int(g["ngrid"]) and np.array_equal(engine.get_table_t3(ng), g["table"])
+    engine.set_particles(g["m"], g["eps"])
+    p = S.params(S.T3, is_periodic=2, L=L, rsim=L / 2, ewald_order=2)
+    assert rel_err(engine.forces(g["x"], p, S.FP64), g["F"]).max() < FP64_TOL
+    # a single-precision build's file holds floats: loaded exactly, as doubles
+    engine.load_table_t3_hdf5(os.path.join(GOLDEN, "t3_table_ng17_f32.h5"))
+    assert np.array_equal(engine.get_table_t3(ng), np.float32(g["table"]).astype(np.float64))
+    g = golden("s1r2_table_o2")
+    nrho, nz = engine.load_table_s1r2_hdf5(os.path.join(GOLDEN, "s1r2_table.h5"))
+    assert (nrho, nz) == tuple(int(v) for v in g["shape"])
+    assert np.array_equal(engine.get_table_s1r2(nrho, nz), g["table"])
+    engine.set_particles(g["m"], g["eps"])
+    assert rel_err(engine.forces(g["x"], s1_params(g, 2, images=0, order=2), S.FP64), g["F"]).max() < FP64_TOL
+    with pytest.raises(S.StepsError) as e:  # the T3 loader rejects an S1xR2 file
+        engine.load_table_t3_hdf5(os.path.join(GOLDEN, "s1r2_table.h5"))
+    assert e.value.code == S.STEPS_E_ARG

@@ -174,3 +174,16 @@ def test_s1r2_table_beyond_radial_extent(port, order):
     s = port.system(2, ps.m, ps.eps, port_params(O, is_periodic=2, L=L, rsim=rsim), table=g["table"], nrho=nrho,
                     nz=nz, order=order)
     assert rel_err(port.forces(s, x), ref.forces()).max() < TOL
+
+
+@pytest.mark.parametrize("size,accuracy,lz_over_L", [(1000, 1000, 0.5), (1000, 1000, 2.6), (257, 64, 5.6)])
+def test_cylindrical_force_table(port, size, accuracy, lz_over_L):
+    """The finite-cylinder radial multiplier (get_cylindrical_force_table,
+    StePS/src/utils.cc:162-228) at the reference's default size and accuracy
+    (1000, 1000; StePS/src/read_paramfile.cc:128-129) and at the half
+    lengths its driver passes (L/2 at IS_PERIODIC = 1, L (IS_PERIODIC + 0.6)
+    above; StePS/src/main.cc:905-917)."""
+    rsim, L = 450.0, 150.0
+    ref = port.cyl_table(rsim, lz_over_L * L, size, accuracy)
+    theirs = O.Ref("s1nl").cyl_table(rsim, lz_over_L * L, size, accuracy)
+    np.testing.assert_allclose(ref, theirs, rtol=TOL, atol=1e-15)
