@@ -220,9 +220,15 @@ int steps_gpu_batch_set(int count, const int *n, const double *const *x, const d
                         const double *const *eps);
 
 /* One force evaluation followed by nsteps fixed-h KDK steps of every
- * realisation. graph = 1 runs it as one persistent work-queue kernel per
- * phase captured into a CUDA graph (autotuned tile shape and block count);
- * graph = 0 runs it as `count` separate plain launches per phase. */
+ * realisation (StePS/src/step.cc:100-312 with g = 1, a = 1, no Hubble drag).
+ * graph = 1 runs the whole of it as ONE persistent kernel, after a single
+ * ordering pass, captured into a CUDA graph: (stage, item) tasks from one
+ * queue, each stage of a realisation starting when its previous stage is
+ * done (bounded waits: STEPS_E_TIMEOUT if one gives up), the kicks, drift and
+ * re-tiling done by the block that completes each tile; tile shape, j-chunk
+ * length and grid size autotuned on the first run. graph = 2 runs it as a
+ * CUDA graph of per-phase kernels (re-ordering every step); graph = 0 as
+ * `count` separate plain launches per phase. */
 int steps_gpu_batch_run(const steps_params *p, int precision, int nsteps, double h, int graph);
 
 /* Downloads realisation k's positions/velocities/forces (any may be NULL). */
@@ -307,6 +313,14 @@ int steps_gpu_host_free(void *p);
  * returns STEPS_E_TIMEOUT, the kernel having left cleanly, and the context
  * stays usable. -1 cancels. One shot. */
 int steps_gpu_test_stall_copy(long long tile_seq);
+
+/* Test hook for the persistent ensemble kernel's bounded waits (no
+ * counterpart in the reference): in the next steps_gpu_batch_run with
+ * graph = 1 (run directly, not from the captured graph), realisation
+ * `realisation` never reports its first stage done, so the waits of its next
+ * stage run out after about a second; the call returns STEPS_E_TIMEOUT and the
+ * context stays usable. -1 cancels. One shot. */
+int steps_gpu_test_stall_ensemble(int realisation);
 
 /* ---- allocation-free entry point ----------------------------------------- */
 

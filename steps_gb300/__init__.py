@@ -243,8 +243,13 @@ class Engine:
         pe = (_dp * k)(*[_d(e) for _, _, e in self._batch])
         self._check(self.lib.steps_gpu_batch_set(k, n, px, pm, pe))
 
-    def batch_run(self, p: Params, precision, nsteps, h, graph=True):
-        self._check(self.lib.steps_gpu_batch_run(C.byref(p), int(precision), int(nsteps), float(h), int(bool(graph))))
+    def batch_run(self, p: Params, precision, nsteps, h, graph=1):
+        """graph: 1 (or True) one persistent kernel in a CUDA graph, 2 a graph of
+        per-phase kernels, 0 (or False) plain per-realisation launches."""
+        self._check(self.lib.steps_gpu_batch_run(C.byref(p), int(precision), int(nsteps), float(h), int(graph)))
+
+    def test_stall_ensemble(self, realisation: int):
+        self._check(self.lib.steps_gpu_test_stall_ensemble(int(realisation)))
 
     def batch_get(self, k):
         n = self._batch[k][1].size

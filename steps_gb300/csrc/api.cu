@@ -80,6 +80,33 @@ void DevBuf::release()
     bytes = 0;
 }
 
+int *kernel_status_word()
+{
+    Ctx &c = g_ctx;
+    if (!c.kstatus.p) {
+        int *w = c.kstatus.ensure<int>(1);
+        STEPS_CUDA(cudaMemsetAsync(w, 0, sizeof(int), c.stream));
+    }
+    return c.kstatus.as<int>();
+}
+
+void check_kernel_status()
+{
+    Ctx &c = g_ctx;
+    if (!c.status_pending || !c.kstatus.p) return;
+    if (!c.kstatus_host) STEPS_CUDA(cudaMallocHost(&c.kstatus_host, sizeof(int)));
+    STEPS_CUDA(cudaMemcpyAsync(c.kstatus_host, c.kstatus.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    STEPS_CUDA(cudaStreamSynchronize(c.stream));
+    c.status_pending = false;
+    if (*c.kstatus_host != 0) {
+        STEPS_CUDA(cudaMemsetAsync(c.kstatus.p, 0, sizeof(int), c.stream));
+        STEPS_CUDA(cudaStreamSynchronize(c.stream));
+        c.F_ni = 0;
+        c.F_valid = false;
+        fail(STEPS_E_TIMEOUT, "a bounded device-side wait gave up (status written by the kernel)");
+    }
+}
+
 void require_init()
 {
     if (g_ctx.device < 0) fail(STEPS_E_STATE, "steps_gpu_init has not been called");

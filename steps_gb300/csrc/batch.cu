@@ -15,9 +15,14 @@
 // FP32x2 R^3 kernel in work-list mode; partial sums go to per-item slots and
 // a reduction adds each i tile's slots in order (deterministic).
 //
-// graph = 1: the whole run -- one force evaluation, then per step kick+drift,
-// re-order, re-tile, force, kick -- is captured once into a CUDA graph and
-// replayed; the tile shape is chosen by timing candidate shapes first.
+// graph = 1: the whole run in ONE persistent kernel (k_ensemble, pair_r3x2.cu)
+// after a single ordering pass, captured into a CUDA graph and replayed:
+// (stage, item) tasks from one queue, a bounded wait per task on its
+// realisation's previous stage, the kicks, drift and tile rebuild done by the
+// block that finishes each tile. The tile shape, the j-chunk length and the
+// grid size are chosen by timing candidates first.
+// graph = 2: the same run as a CUDA graph of per-phase kernels (per step:
+// kick+drift, re-order, re-tile, work-list force, reduction, kick).
 // graph = 0: the same work as `count` separate single-realisation force calls
 // (and KDK kernels) per phase, for comparison.
 #include <algorithm>
@@ -43,11 +48,20 @@ struct Batch {
     DevBuf tslot;                 // int2 per tile: first partial slot, number of slots
     DevBuf part, counter, err;
     int T = 0, ntiles = 0, nitems = 0, threads = 0, ipt = 0, grid = 0;
+    int jmax = 256;  // j tiles per work item at most
     long long graph_kernels = 0;
     int nmax = 0;  // largest realisation
-    bool tuned = false;
+    bool tuned = false;     // per-phase graph shape
+    bool ens_tuned = false; // persistent kernel shape, j-chunk length, grid
+    int threads_pp = 128, ipt_pp = 2;  // per-phase graph shape
+    int ens_threads = 128, ens_ipt = 2, ens_jmax = 256, ens_grid = 0;
+    double ens_frac = 1.0;
+    // persistent path: the second tile buffer, per-tile realisation, counters
+    DevBuf pack2, soa2, resid2, meta2, sub2;
+    DevBuf tile_rel, rel_ntiles, ens_ctl;
+    int stall_rel = -1;  // test hook for the next persistent run (one shot)
     cudaGraphExec_t exec = nullptr;
-    int graph_steps = -1;
+    int graph_steps = -1, graph_mode = 0;
     double graph_h = 0.0;
 };
 
@@ -111,10 +125,11 @@ __global__ void k_batch_reduce(const double *__restrict__ part, const int2 *__re
 }
 
 // Tile descriptors and the work list for tile size T (host side, once per shape).
-void plan(Batch &b, int threads, int ipt)
+void plan(Batch &b, int threads, int ipt, int jmax = 256)
 {
     Ctx &c = ctx();
     const int T = threads * ipt;
+    b.jmax = jmax;
     std::vector<int> tstart(b.count), nt(b.count);
     std::vector<int2> desc;
     for (int k = 0; k < b.count; k++) {
@@ -123,14 +138,17 @@ void plan(Batch &b, int threads, int ipt)
         for (int t = 0; t < nt[k]; t++) desc.push_back(make_int2(b.off[k] + t * T, std::min(T, b.n[k] - t * T)));
     }
     b.ntiles = (int)desc.size();
-    // Items: per realisation i tiles x j chunks of at most 256 tiles; largest realisations first.
+    // Items: per realisation i tiles x j chunks of at most jmax tiles; largest realisations first.
     std::vector<int> order(b.count);
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(), [&](int a, int d) { return b.n[a] > b.n[d]; });
     std::vector<int4> items;
     std::vector<int2> tslot(b.ntiles);
+    std::vector<int> trel(b.ntiles);
+    for (int k = 0; k < b.count; k++)
+        for (int t = 0; t < nt[k]; t++) trel[tstart[k] + t] = k;
     for (int k : order) {
-        const int S = div_up(nt[k], 256);
+        const int S = div_up(nt[k], jmax);
         const int per = div_up(nt[k], S);
         for (int I = 0; I < nt[k]; I++) {
             const int gI = tstart[k] + I;
@@ -151,6 +169,10 @@ void plan(Batch &b, int threads, int ipt)
                                cudaMemcpyHostToDevice, c.stream));
     STEPS_CUDA(cudaMemcpyAsync(b.tslot.ensure<int2>(tslot.size()), tslot.data(), tslot.size() * sizeof(int2),
                                cudaMemcpyHostToDevice, c.stream));
+    STEPS_CUDA(cudaMemcpyAsync(b.tile_rel.ensure<int>(trel.size()), trel.data(), trel.size() * sizeof(int),
+                               cudaMemcpyHostToDevice, c.stream));
+    STEPS_CUDA(cudaMemcpyAsync(b.rel_ntiles.ensure<int>(nt.size()), nt.data(), nt.size() * sizeof(int),
+                               cudaMemcpyHostToDevice, c.stream));
     b.ts.pack.ensure<float4>(padded);
     b.ts.eps.ensure<float>(padded);
     b.ts.meta.ensure<float4>(2 * (size_t)b.ntiles);
@@ -158,6 +180,12 @@ void plan(Batch &b, int threads, int ipt)
     b.ts.resid.ensure<float4>(padded);
     b.ts.soa.ensure<float4>(padded);
     b.ts.sub.ensure<float4>(2 * (padded / SUBTILE));
+    b.pack2.ensure<float4>(padded);
+    b.soa2.ensure<float4>(padded);
+    b.resid2.ensure<float4>(padded);
+    b.meta2.ensure<float4>(2 * (size_t)b.ntiles);
+    b.sub2.ensure<float4>(2 * (padded / SUBTILE));
+    b.ens_ctl.ensure<unsigned>(1 + (size_t)b.ntiles + b.count);
     b.part.ensure<double>((size_t)b.nitems * T * 3);
     b.T = T;
     b.threads = threads;
@@ -170,9 +198,9 @@ void plan(Batch &b, int threads, int ipt)
     STEPS_CUDA(cudaStreamSynchronize(c.stream));
 }
 
-// One batched force evaluation on the resident positions (stream-ordered; no
-// host synchronisation, so it can be captured into a graph).
-void batch_forces(Batch &b)
+// Orders every realisation (one sort) and builds the tiles into the first
+// tile buffer (and, for the persistent kernel, the second one as well).
+void batch_order(Batch &b, bool both_buffers)
 {
     Ctx &c = ctx();
     cudaStream_t st = c.stream;
@@ -192,6 +220,20 @@ void batch_forces(Batch &b)
                      b.ts.pack.as<float4>(), b.ts.eps.as<float>(), b.ts.meta.as<float4>(), b.ts.idx.as<uint32_t>(),
                      PAD_J, b.ts.resid.as<float4>(), b.ts.soa.as<float>(), b.tdesc.as<int2>(), b.ntiles, st,
                      b.ts.sub.as<float4>());
+    if (both_buffers)
+        tile_build_range(b.x.as<double>(), b.m64.as<double>(), b.eps64.as<double>(), b.ts.perm(), b.ntot, b.T,
+                         b.pack2.as<float4>(), b.ts.eps.as<float>(), b.meta2.as<float4>(), nullptr, PAD_J,
+                         b.resid2.as<float4>(), b.soa2.as<float>(), b.tdesc.as<int2>(), b.ntiles, st,
+                         b.sub2.as<float4>());
+}
+
+// One batched force evaluation on the resident positions (stream-ordered; no
+// host synchronisation, so it can be captured into a graph).
+void batch_forces(Batch &b)
+{
+    Ctx &c = ctx();
+    cudaStream_t st = c.stream;
+    batch_order(b, false);
 
     mixed::MixedArgs a{};
     a.stall_seq = -1;
@@ -217,6 +259,107 @@ void batch_forces(Batch &b)
                                                                 b.ts.idx.as<uint32_t>(), b.ntiles * b.T, b.T,
                                                                 b.F.as<double>());
     note_launch("k_batch_reduce");
+}
+
+// The whole run in one persistent kernel (stream-ordered, capturable): one
+// ordering pass that builds both tile buffers, the counters zeroed, then
+// k_ensemble over nsteps + 1 stages.
+void ensemble_run(Batch &b, int nsteps, double h, int stall_rel)
+{
+    Ctx &c = ctx();
+    cudaStream_t st = c.stream;
+    batch_order(b, true);
+    unsigned *ctl = b.ens_ctl.as<unsigned>();
+    STEPS_CUDA(cudaMemsetAsync(ctl, 0, sizeof(unsigned) * (1 + (size_t)b.ntiles + b.count), st));
+    mixed::EnsembleArgs e{};
+    float4 *pk[2] = {b.ts.pack.as<float4>(), b.pack2.as<float4>()};
+    float *so[2] = {b.ts.soa.as<float>(), b.soa2.as<float>()};
+    float4 *re[2] = {b.ts.resid.as<float4>(), b.resid2.as<float4>()};
+    float4 *me[2] = {b.ts.meta.as<float4>(), b.meta2.as<float4>()};
+    float4 *su[2] = {b.ts.sub.as<float4>(), b.sub2.as<float4>()};
+    for (int k = 0; k < 2; k++) {
+        e.pack[k] = e.pack_w[k] = pk[k];
+        e.soa[k] = e.soa_w[k] = so[k];
+        e.resid[k] = e.resid_w[k] = re[k];
+        e.meta[k] = e.meta_w[k] = me[k];
+        e.sub[k] = e.sub_w[k] = su[k];
+    }
+    e.jeps = b.ts.eps.as<float>();
+    e.epsf_w = b.ts.eps.as<float>();
+    e.jidx = b.ts.idx.as<uint32_t>();
+    e.items = b.items.as<int4>();
+    e.nitems = b.nitems;
+    e.nstages = nsteps + 1;
+    e.tile_rel = b.tile_rel.as<int>();
+    e.tdesc = b.tdesc.as<int2>();
+    e.tslot = b.tslot.as<int2>();
+    e.rel_ntiles = b.rel_ntiles.as<int>();
+    e.perm = b.ts.perm();
+    e.part = b.part.as<double>();
+    e.queue = ctl;
+    e.tile_cnt = ctl + 1;
+    e.rel_done = ctl + 1 + b.ntiles;
+    e.x = b.x.as<double>();
+    e.v = b.v.as<double>();
+    e.F = b.F.as<double>();
+    e.m64 = b.m64.as<double>();
+    e.eps64 = b.eps64.as<double>();
+    e.h = h;
+    e.guard2 = c.shape.guard * c.shape.guard;
+    e.status = kernel_status_word();
+    e.stall_rel = stall_rel;
+    mixed::EnsembleFn fn = ensemble_kernel(b.threads, b.ipt);
+    if (!fn) fail(STEPS_E_ARG, "batch: unsupported kernel shape");
+    fn<<<b.ens_grid, b.threads, 0, st>>>(e);
+    note_launch("k_ensemble");
+    c.status_pending = true;
+}
+
+// Plans the work list for the persistent kernel's shape and sizes its grid:
+// `frac` of the blocks that fit on the GPU at once.
+void ensemble_plan(Batch &b, int threads, int ipt, int jmax, double frac)
+{
+    Ctx &c = ctx();
+    plan(b, threads, ipt, jmax);
+    mixed::EnsembleFn fn = ensemble_kernel(threads, ipt);
+    if (!fn) fail(STEPS_E_ARG, "batch: unsupported kernel shape");
+    int occ = 0;
+    STEPS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, threads, 0));
+    const int resident = c.nsm * std::max(occ, 1);
+    b.ens_grid = std::max(1, std::min(b.nitems, (int)(frac * resident)));
+}
+
+// Times one force evaluation (a one-stage run) per candidate tile shape,
+// j-chunk length and grid size, and keeps the fastest.
+void ensemble_tune(Batch &b)
+{
+    Ctx &c = ctx();
+    static const int shapes[][2] = {{128, 2}, {128, 1}, {256, 1}, {64, 2}};
+    static const int jmaxes[] = {64, 256};
+    static const double fracs[] = {1.0, 0.75};
+    float best = 1e30f;
+    int bt = 128, bi = 2, bj = 256;
+    double bf = 1.0;
+    for (auto &sh : shapes)
+        for (int jm : jmaxes)
+            for (double fr : fracs) {
+                ensemble_plan(b, sh[0], sh[1], jm, fr);
+                ensemble_run(b, 0, 0.0, -1);  // warm
+                STEPS_CUDA(cudaEventRecord(c.marks[12], c.stream));
+                ensemble_run(b, 0, 0.0, -1);
+                STEPS_CUDA(cudaEventRecord(c.marks[13], c.stream));
+                STEPS_CUDA(cudaEventSynchronize(c.marks[13]));
+                float ms = 0;
+                STEPS_CUDA(cudaEventElapsedTime(&ms, c.marks[12], c.marks[13]));
+                if (ms < best) { best = ms; bt = sh[0]; bi = sh[1]; bj = jm; bf = fr; }
+            }
+    check_kernel_status();
+    ensemble_plan(b, bt, bi, bj, bf);
+    b.ens_threads = bt;
+    b.ens_ipt = bi;
+    b.ens_jmax = bj;
+    b.ens_frac = bf;
+    b.ens_tuned = true;
 }
 
 void batch_steps(Batch &b, int nsteps, double h)
@@ -291,7 +434,8 @@ void batch_release()
     DevBuf *bufs[] = {&b->x, &b->v, &b->F, &b->m64, &b->eps64, &b->rel, &b->bbox, &b->tdesc, &b->items, &b->tslot,
                       &b->part, &b->counter, &b->err, &b->ts.keys[0], &b->ts.keys[1], &b->ts.vals[0], &b->ts.vals[1],
                       &b->ts.hist, &b->ts.pack, &b->ts.eps, &b->ts.meta, &b->ts.idx, &b->ts.resid, &b->ts.soa,
-                      &b->ts.sub};
+                      &b->ts.sub, &b->pack2, &b->soa2, &b->resid2, &b->meta2, &b->sub2, &b->tile_rel,
+                      &b->rel_ntiles, &b->ens_ctl};
     for (DevBuf *d : bufs) d->release();
     delete b;
     c.batch = nullptr;
@@ -400,7 +544,25 @@ int steps_gpu_batch_run(const steps_params *p, int precision, int nsteps, double
                 return;
             }
             if (a.precision != STEPS_MIXED) fail(STEPS_E_ARG, "batch graph: mixed precision only");
-            if (!b.tuned) {
+            if (a.graph != 1 && a.graph != 2) fail(STEPS_E_ARG, "batch: graph must be 0, 1 or 2");
+            const bool persistent = a.graph == 1;
+            if (persistent && b.stall_rel >= 0) {
+                // the test hook: one direct (uncaptured) run with the stall
+                const int k = b.stall_rel;
+                b.stall_rel = -1;
+                if (!b.ens_tuned) ensemble_tune(b);
+                else ensemble_plan(b, b.ens_threads, b.ens_ipt, b.ens_jmax, b.ens_frac);
+                release_graph(b);
+                ensemble_run(b, a.nsteps, a.h, k);
+                STEPS_CUDA(cudaStreamSynchronize(c.stream));
+                check_kernel_status();
+                return;
+            }
+            if (persistent && !b.ens_tuned) {
+                ensemble_tune(b);
+                release_graph(b);
+            }
+            if (!persistent && !b.tuned) {
                 // Time one batched force per candidate shape, keep the fastest.
                 static const int shapes[][2] = {{128, 2}, {64, 4}, {128, 1}, {256, 1}, {128, 4}, {256, 2}};
                 float best = 1e30f;
@@ -417,17 +579,24 @@ int steps_gpu_batch_run(const steps_params *p, int precision, int nsteps, double
                     if (ms < best) { best = ms; bt = s[0]; bi = s[1]; }
                 }
                 plan(b, bt, bi);
+                b.threads_pp = bt;
+                b.ipt_pp = bi;
                 b.tuned = true;
                 release_graph(b);
             }
-            if (!b.exec || b.graph_steps != a.nsteps || b.graph_h != a.h) {
+            if (!b.exec || b.graph_steps != a.nsteps || b.graph_h != a.h || b.graph_mode != a.graph) {
                 release_graph(b);
-                batch_forces(b);  // sizes every buffer before capture
+                // the plan of the chosen path (the two paths keep their own shapes)
+                if (persistent) ensemble_plan(b, b.ens_threads, b.ens_ipt, b.ens_jmax, b.ens_frac);
+                else plan(b, b.threads_pp, b.ipt_pp);
+                if (!persistent) batch_forces(b);  // sizes every buffer before capture
+                kernel_status_word();              // allocated outside the capture
                 STEPS_CUDA(cudaStreamSynchronize(c.stream));
                 cudaGraph_t g;
                 STEPS_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
                 try {
-                    batch_steps(b, a.nsteps, a.h);
+                    if (persistent) ensemble_run(b, a.nsteps, a.h, -1);
+                    else batch_steps(b, a.nsteps, a.h);
                 } catch (...) {
                     cudaGraph_t dummy;
                     cudaStreamEndCapture(c.stream, &dummy);
@@ -441,12 +610,28 @@ int steps_gpu_batch_run(const steps_params *p, int precision, int nsteps, double
                 STEPS_CUDA(e);
                 b.graph_steps = a.nsteps;
                 b.graph_h = a.h;
+                b.graph_mode = a.graph;
             }
             STEPS_CUDA(cudaGraphLaunch(b.exec, c.stream));
             add_launches(b.graph_kernels);  // the kernels the graph runs
+            if (persistent) c.status_pending = true;
             STEPS_CUDA(cudaStreamSynchronize(c.stream));
+            check_kernel_status();
         },
         &args);
+}
+
+int steps_gpu_test_stall_ensemble(int realisation)
+{
+    return run_guarded(
+        [](void *vp) {
+            const int k = *static_cast<int *>(vp);
+            Batch *b = ctx().batch;
+            if (!b) fail(STEPS_E_STATE, "no batch: call steps_gpu_batch_set first");
+            if (k < -1 || k >= b->count) fail(STEPS_E_ARG, "test_stall_ensemble: no such realisation");
+            b->stall_rel = k;
+        },
+        &realisation);
 }
 
 int steps_gpu_batch_get(int k, double *x, double *v, double *F)

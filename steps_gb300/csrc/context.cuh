@@ -28,6 +28,7 @@ struct Ctx {
     DevBuf bbox, counter, status, flush, peaks;
     DevBuf kstatus;                  // int written by kernels whose bounded waits give up
     int *kstatus_host = nullptr;     // page-locked mirror of kstatus
+    bool status_pending = false;     // a kernel that can write kstatus ran since it was last read
     long long stall_seq = -1;        // test hook for the next pipelined launch (one shot)
     TileSet tj, ti;                  // j set (all particles) and i subset tiles
 
@@ -61,6 +62,13 @@ struct Ctx {
 
 Ctx &ctx();
 void require_init();
+// The device status word kernels with bounded waits write STEPS_E_TIMEOUT to
+// (zero until a wait gives up; zeroed when allocated).
+int *kernel_status_word();
+// Reads that word (synchronising the stream) when such a kernel ran since it
+// was last read; fails with STEPS_E_TIMEOUT, clearing the word and the
+// resident force range, when a wait gave up.
+void check_kernel_status();
 // Runs body(arg), turning a thrown Error into its status code (and message).
 int run_guarded(void (*body)(void *), void *arg);
 void batch_release();

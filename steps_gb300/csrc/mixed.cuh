@@ -322,6 +322,46 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned by
 
 using KernelFn = void (*)(MixedArgs);
 
+// The persistent ensemble kernel (pair_r3x2.cu): every force evaluation and
+// KDK step of a batch of realisations in one launch. Tasks are (stage, item)
+// for stage 0 .. nstages - 1 (stage 0: the initial force; stage s >= 1: the
+// force after step s) over the batch's work list, largest realisation first.
+// Tile data that the run rewrites (offsets, residuals, metadata, sub-tile
+// boxes) are double-buffered: stage s reads buffer s & 1.
+struct EnsembleArgs {
+    const float4 *pack[2];  // i offsets (x - c, y - c, z - c, m)
+    const float *soa[2];    // tile-blocked SoA j copy
+    const float4 *resid[2];
+    const float4 *meta[2];
+    const float4 *sub[2];
+    float4 *pack_w[2];      // the same buffers, written by the rebuild
+    float *soa_w[2];
+    float4 *resid_w[2];
+    float4 *meta_w[2];
+    float4 *sub_w[2];
+    const float *jeps;      // softening (constant over the run)
+    const uint32_t *jidx;   // original index of each padded position (constant)
+    float *epsf_w;
+    const int4 *items;      // work list: i tile, j tile begin, j tile end, partial slot
+    int nitems, nstages;
+    const int *tile_rel;    // realisation of each tile
+    const int2 *tdesc;      // per tile: first sorted position, particle count
+    const int2 *tslot;      // per tile: first partial slot, number of slots
+    const int *rel_ntiles;  // tiles of each realisation
+    const uint32_t *perm;   // sorted position -> original index
+    double *part;           // partial slots [slot][T][3]
+    unsigned *queue;        // task counter
+    unsigned *tile_cnt;     // per tile: items finished, over all stages
+    unsigned *rel_done;     // per realisation: tiles finished (forces, kicks, drift, rebuild), over all stages
+    double *x, *v, *F;      // caller-order FP64 positions, velocities, forces
+    const double *m64, *eps64;
+    double h;               // fixed step; acceleration g F a^-3 - 2 H v with g = 1, a = 1, H = 0
+    float guard2;
+    int *status;            // STEPS_E_TIMEOUT when a stage wait gave up
+    int stall_rel;          // test hook: this realisation's stage-0 tiles are never reported done (-1: none)
+};
+using EnsembleFn = void (*)(EnsembleArgs);
+
 }  // namespace mixed
 
 // pair_t3.cu: T^3 kernel for a shape (dynamic shared memory returned) and its
@@ -337,6 +377,8 @@ inline int r3x2_occ(int variant) { return variant == 2 ? 768 : variant == 3 ? 10
 // copies through an mbarrier ring (variant 4).
 mixed::KernelFn r3x2_pipe_kernel(int threads, int ipt);
 constexpr int R3_VARIANTS = 5;  // 0 scalar, 1-3 packed, 4 packed + bulk-copy pipeline
+// pair_r3x2.cu: the persistent ensemble kernel for a shape.
+mixed::EnsembleFn ensemble_kernel(int threads, int ipt);
 // S1xR2 with the (rho, z) table (IS_PERIODIC >= 2, no explicit images).
 mixed::KernelFn s1tab_kernel(const KParams &kp, int threads, int ipt);
 void s1tab_args(mixed::MixedArgs &a, const KParams &kp, const Tables &tb, cudaStream_t st);

@@ -559,7 +559,7 @@ void forces_mixed(const KParams &kp, const Tables &tb, const double *x, const do
     if (kp.topology == STEPS_T3) t3_args(a, kp, tb, st);
     if (s1tab) s1tab_args(a, kp, tb, st);
 
-    a.status = c.kstatus.ensure<int>(1);
+    a.status = kernel_status_word();
     a.stall_seq = c.stall_seq;
     c.stall_seq = -1;
     STEPS_CUDA(cudaMemsetAsync(a.counter, 0, sizeof(unsigned), st));

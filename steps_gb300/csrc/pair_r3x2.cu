@@ -15,6 +15,7 @@
 #include "common.cuh"
 #include "context.cuh"
 #include "mixed.cuh"
+#include "tile.cuh"
 
 namespace steps {
 
@@ -58,25 +59,24 @@ __device__ __forceinline__ float pin_to(float v, int dep)
 // from the sub-tile boxes: lane s classifies sub-tile s, a ballot gathers the
 // warp-uniform mask, and runs of far sub-tiles take the packed loop while
 // near (or coarse-scale) sub-tiles take the scalar double-float path.
+// mJ0: tile J's FP32 centre and largest softening (its first metadata float4).
 template <int BLOCK, int IPT>
-__device__ __forceinline__ void r3x2_tile(const MixedArgs &a, int J, const float *sxb, const float *seb,
+__device__ __forceinline__ void r3x2_tile(float4 mJ0, float guard2, const float *sxb, const float *seb,
                                           const uint32_t *sidb, const float4 *sresb, const float4 *ssubb, float4 mI0,
-                                          float4 wc, float4 wh,
-                                          float wemax, const float *xi, const float *yi, const float *zi,
-                                          const float *ei, const float *lx, const float *ly, const float *lz,
-                                          const uint32_t *ii, double *ax, double *ay, double *az)
+                                          float4 wc, float4 wh, float wemax, const float *xi, const float *yi,
+                                          const float *zi, const float *ei, const float *lx, const float *ly,
+                                          const float *lz, const uint32_t *ii, double *ax, double *ay, double *az)
 {
     constexpr int T = BLOCK * IPT;
     constexpr int NS = T / SUBTILE;  // 4 .. 32 sub-tiles
     constexpr unsigned ALL = NS == 32 ? 0xffffffffu : (1u << NS) - 1u;
-    const float4 mJ0 = __ldg(a.jmeta + 2 * J);
     float eOx, eOy, eOz;
     const float dOx = two_diff(mJ0.x, mI0.x, eOx), dOy = two_diff(mJ0.y, mI0.y, eOy),
                 dOz = two_diff(mJ0.z, mI0.z, eOz);
     // Near field / coarse FP32 scale per (warp, sub-tile), warp-uniform.
     const int lane = threadIdx.x & 31;
     bool f = false;
-    if (lane < NS) f = warp_full_sub(dOx, dOy, dOz, ssubb[2 * lane], ssubb[2 * lane + 1], wc, wh, wemax, a.guard2);
+    if (lane < NS) f = warp_full_sub(dOx, dOy, dOz, ssubb[2 * lane], ssubb[2 * lane + 1], wc, wh, wemax, guard2);
     const unsigned full = __ballot_sync(0xffffffffu, f) & ALL;
     const float *X = sxb;
     const float *Y = X + T;
@@ -266,7 +266,7 @@ __device__ __forceinline__ void r3x2_body(const MixedArgs &a)
             }
             __syncthreads();
 
-            r3x2_tile<BLOCK, IPT>(a, J, sx[buf], se[buf], sid[buf], sres[buf], ssub[buf], mI0, wc, wh, wemax, xi, yi,
+            r3x2_tile<BLOCK, IPT>(__ldg(a.jmeta + 2 * J), a.guard2, sx[buf], se[buf], sid[buf], sres[buf], ssub[buf], mI0, wc, wh, wemax, xi, yi,
                                   zi, ei, lx, ly, lz, ii, ax, ay, az);
             __syncthreads();
         }
@@ -387,7 +387,7 @@ __device__ __forceinline__ void r3x2_pipe_body(const MixedArgs &a)
                 if (lane == 0) abort_block();
                 break;
             }
-            r3x2_tile<BLOCK, IPT>(a, J, sx[st], se[st], sid[st], sres[st], ssub[st], mI0, wc, wh, wemax, xi, yi, zi, ei,
+            r3x2_tile<BLOCK, IPT>(__ldg(a.jmeta + 2 * J), a.guard2, sx[st], se[st], sid[st], sres[st], ssub[st], mI0, wc, wh, wemax, xi, yi, zi, ei,
                                   lx, ly, lz, ii, ax, ay, az);
             __syncwarp();
             if (lane == 0) mbar_arrive(&empty[st]);
@@ -433,7 +433,205 @@ __global__ void __launch_bounds__(BLOCK, OCC / BLOCK) k_pair_r3x2_occ(MixedArgs 
     r3x2_body<BLOCK, IPT, false>(a);
 }
 
+// ---- persistent ensemble kernel --------------------------------------------
+//
+// One launch runs every stage of a batch run (EnsembleArgs): the initial force
+// evaluation and, per KDK step, the force at the drifted positions. A block
+// takes (stage, item) tasks from one atomic counter in queue order (stage by
+// stage, each stage's items largest realisation first). A stage-s task of
+// realisation k may start once all of k's tiles have been finished at stage
+// s - 1 -- a bounded wait, which in queue order rarely waits at all, since
+// k's previous-stage items were queued long before. The block that completes
+// the last item of an i tile at stage s adds the tile's partial slots in
+// order (deterministic), writes F, applies the kick of the step that stage
+// ends (StePS/src/step.cc:256-262), then the next step's kick and drift
+// (step.cc:131-149), and rebuilds the tile into the other buffer; then it
+// counts the tile done for its realisation. Particles keep the order of the
+// initial sort for the whole run (the forces do not depend on the order).
+//
+// A wait that gives up (about a second) records STEPS_E_TIMEOUT; every block
+// then stops taking tasks, and waits in progress give up at once.
+
+// Bounded spin on a counter another block increments: true once it reaches
+// target; false after MBAR_WAIT_CYCLES or as soon as the status word is set.
+__device__ __forceinline__ bool wait_counter(const unsigned *cnt, unsigned target, const int *status)
+{
+    const volatile unsigned *c = cnt;
+    const volatile int *st = status;
+    if (*c >= target) return true;
+    const long long t0 = clock64();
+    while (*c < target)
+        if (*st != 0 || clock64() - t0 > MBAR_WAIT_CYCLES) return false;
+    return true;
+}
+
+template <int BLOCK, int IPT>
+__device__ __forceinline__ void ensemble_finish_tile(const EnsembleArgs &e, int I, int stage)
+{
+    constexpr int T = BLOCK * IPT;
+    const int tid = threadIdx.x;
+    const int2 sl = __ldg(e.tslot + I), td = __ldg(e.tdesc + I);
+    const bool kick2 = stage >= 1, kick1 = stage < e.nstages - 1;
+    const double h2 = e.h / 2.0;
+    for (int p = tid; p < T; p += BLOCK) {
+        const uint32_t o = __ldg(e.jidx + (size_t)I * T + p);
+        if (o == 0xffffffffu) continue;  // padding
+        double f[3] = {0.0, 0.0, 0.0};
+        for (int s = 0; s < sl.y; s++) {
+            const double *pc = e.part + ((size_t)(sl.x + s) * T + p) * 3;
+            f[0] += __ldcg(pc);
+            f[1] += __ldcg(pc + 1);
+            f[2] += __ldcg(pc + 2);
+        }
+        for (int c = 0; c < 3; c++) {
+            const size_t q = 3 * (size_t)o + c;
+            e.F[q] = f[c];
+            double vv = __ldcg(e.v + q);
+            // acceleration g F a^-3 - 2 H v at g = 1, a = 1, H = 0, as the batch's KDK kernels evaluate it
+            if (kick2) vv += (1.0 * f[c] * 1.0 - 2.0 * 0.0 * vv) * h2;
+            if (kick1) {
+                vv = vv + (1.0 * f[c] * 1.0 - 2.0 * 0.0 * vv) * h2;
+                e.x[q] = __ldcg(e.x + q) + vv * e.h;
+            }
+            e.v[q] = vv;
+        }
+    }
+    __syncthreads();
+    if (kick1) {
+        const int nb = (stage + 1) & 1;
+        build_tile<BLOCK, true>(I, td.x, td.y, e.x, e.m64, e.eps64, e.perm, T, e.pack_w[nb], e.epsf_w, e.meta_w[nb],
+                                nullptr, 0xffffffffu, e.resid_w[nb], e.soa_w[nb], e.sub_w[nb]);
+    }
+    __syncthreads();
+    if (tid == 0) {
+        __threadfence();
+        const int k = __ldg(e.tile_rel + I);
+        if (!(stage == 0 && k == e.stall_rel)) atomicAdd(e.rel_done + k, 1u);
+    }
+}
+
+template <int BLOCK, int IPT>
+__global__ void __launch_bounds__(BLOCK, BLOCK <= 128 && IPT <= 2 ? 640 / BLOCK : 1) k_ensemble(EnsembleArgs e)
+{
+    constexpr int T = BLOCK * IPT;
+    __shared__ __align__(16) float sx[2][4 * T];
+    __shared__ __align__(16) float se[2][T];
+    __shared__ __align__(16) uint32_t sid[2][T];
+    __shared__ __align__(16) float4 sres[2][T];
+    __shared__ __align__(16) float4 ssub[2][2 * (T / SUBTILE)];
+    __shared__ __align__(16) float4 smeta[2];  // the staged j tile's centre and largest softening
+    __shared__ int s_task, s_last;
+    const int tid = threadIdx.x;
+    const int ntasks = e.nitems * e.nstages;
+    // A j tile with its metadata, in one cp.async group, all through L2.
+    auto stage_j = [&](const MixedArgs &sa, const float4 *jmeta, int J, int buf) {
+        if (tid == 0) cp_async16(&smeta[buf], jmeta + 2 * J);
+        stage_soa<BLOCK, IPT>(sa, J, sx[buf], se[buf], sid[buf], sres[buf], ssub[buf]);
+    };
+
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) {
+            const volatile int *st = e.status;
+            int task = *st != 0 ? ntasks : (int)atomicAdd(e.queue, 1u);
+            if (task < ntasks && task >= e.nitems) {  // stage >= 1: wait for the previous stage of this realisation
+                const int stage = task / e.nitems;
+                const int k = __ldg(e.tile_rel + __ldg(e.items + task % e.nitems).x);
+                if (!wait_counter(e.rel_done + k, (unsigned)(__ldg(e.rel_ntiles + k) * stage), e.status)) {
+                    atomicExch(e.status, STEPS_E_TIMEOUT);
+                    task = ntasks;
+                }
+            }
+            __threadfence();
+            s_task = task;
+        }
+        __syncthreads();
+        const int task = s_task;
+        if (task >= ntasks) break;
+        const int stage = task / e.nitems;
+        const int b = stage & 1;
+        const int4 d = __ldg(e.items + task % e.nitems);
+        const int I = d.x, J0 = d.y, J1 = d.z;
+        const float4 *ipack = e.pack[b], *ilo = e.resid[b], *imeta = e.meta[b];
+
+        const float4 mI0 = __ldcg(imeta + 2 * I);
+        float xi[IPT], yi[IPT], zi[IPT], ei[IPT], lx[IPT], ly[IPT], lz[IPT];
+        uint32_t ii[IPT];
+        double ax[IPT], ay[IPT], az[IPT];
+#pragma unroll
+        for (int k = 0; k < IPT; k++) {
+            const size_t q = (size_t)I * T + k * BLOCK + tid;
+            const float4 p = __ldcg(ipack + q);
+            xi[k] = p.x;
+            yi[k] = p.y;
+            zi[k] = p.z;
+            ei[k] = __ldg(e.jeps + q);
+            ii[k] = __ldg(e.jidx + q);
+            const float4 l = __ldcg(ilo + q);
+            lx[k] = l.x;
+            ly[k] = l.y;
+            lz[k] = l.z;
+            ax[k] = ay[k] = az[k] = 0.0;
+        }
+        float4 wc, wh;
+        warp_box<IPT>(xi, yi, zi, wc, wh);
+        const float wemax = warp_eps_max<IPT>(ei);
+
+        MixedArgs a;  // the fields stage_soa reads
+        a.jsoa = e.soa[b];
+        a.jeps = e.jeps;
+        a.jidx = e.jidx;
+        a.jres = e.resid[b];
+        a.jsub = e.sub[b];
+        if (J0 < J1) stage_j(a, e.meta[b], J0, 0);
+        for (int J = J0; J < J1; ++J) {
+            const int buf = (J - J0) & 1;
+            if (J + 1 < J1) {
+                stage_j(a, e.meta[b], J + 1, buf ^ 1);
+                cp_wait<1>();
+            } else {
+                cp_wait<0>();
+            }
+            __syncthreads();
+            r3x2_tile<BLOCK, IPT>(smeta[buf], e.guard2, sx[buf], se[buf], sid[buf], sres[buf], ssub[buf], mI0, wc, wh,
+                                  wemax, xi, yi, zi, ei, lx, ly, lz, ii, ax, ay, az);
+            __syncthreads();
+        }
+
+        double *o = e.part + (size_t)d.w * 3 * T;
+#pragma unroll
+        for (int k = 0; k < IPT; k++) {
+            const size_t q = k * BLOCK + tid;
+            o[3 * q] = ax[k];
+            o[3 * q + 1] = ay[k];
+            o[3 * q + 2] = az[k];
+        }
+        __threadfence();
+        __syncthreads();
+        if (tid == 0) {
+            const unsigned slots = (unsigned)__ldg(e.tslot + I).y;
+            s_last = atomicAdd(e.tile_cnt + I, 1u) == slots * (unsigned)(stage + 1) - 1u;
+        }
+        __syncthreads();
+        if (s_last) {
+            __threadfence();
+            ensemble_finish_tile<BLOCK, IPT>(e, I, stage);
+        }
+    }
+}
+
 }  // namespace
+
+EnsembleFn ensemble_kernel(int threads, int ipt)
+{
+#define STEPS_SHAPE(B, P) \
+    if (threads == B && ipt == P) return k_ensemble<B, P>;
+    STEPS_SHAPE(64, 1) STEPS_SHAPE(64, 2) STEPS_SHAPE(64, 4)
+    STEPS_SHAPE(128, 1) STEPS_SHAPE(128, 2) STEPS_SHAPE(128, 4)
+    STEPS_SHAPE(256, 1) STEPS_SHAPE(256, 2)
+#undef STEPS_SHAPE
+    return nullptr;
+}
 
 KernelFn r3x2_pipe_kernel(int threads, int ipt)
 {

@@ -30,22 +30,25 @@ def oracle_run(port, ps, nsteps):
     return x, v, F
 
 
-def test_batch_graph_and_plain_match_oracle(engine, port):
+@pytest.mark.parametrize("mode", [1, 2])
+def test_batch_graph_and_plain_match_oracle(engine, port, mode):
+    """mode 1: the whole run in one persistent kernel under a CUDA graph;
+    mode 2: a CUDA graph of per-phase kernels."""
     sets = ensemble()
     p = S.params(S.R3)
     engine.set_variant(1)
     try:
         engine.batch_set([s.x for s in sets], [s.m for s in sets], [s.eps for s in sets])
-        engine.batch_run(p, S.MIXED, 2, DT, graph=True)
+        engine.batch_run(p, S.MIXED, 2, DT, graph=mode)
         graph = [engine.batch_get(k) for k in range(len(sets))]
-        engine.batch_run(p, S.MIXED, 2, DT, graph=True)  # replays the captured graph: 4 steps in all
+        engine.batch_run(p, S.MIXED, 2, DT, graph=mode)  # replays the captured graph: 4 steps in all
         graph4 = [engine.batch_get(k) for k in range(len(sets))]
         engine.batch_set([s.x for s in sets], [s.m for s in sets], [s.eps for s in sets])
-        engine.batch_run(p, S.MIXED, 2, DT, graph=False)
+        engine.batch_run(p, S.MIXED, 2, DT, graph=0)
         plain = [engine.batch_get(k) for k in range(len(sets))]
         # same sizes registered again: new data, the tuned plan and graph are reused
         engine.batch_set([s.x for s in sets], [s.m for s in sets], [s.eps for s in sets])
-        engine.batch_run(p, S.MIXED, 2, DT, graph=True)
+        engine.batch_run(p, S.MIXED, 2, DT, graph=mode)
         again = [engine.batch_get(k) for k in range(len(sets))]
     finally:
         engine.set_variant(0)
