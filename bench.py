@@ -61,7 +61,12 @@ LOOPS = ["fp32", "fp32x2", "fp32x2 (768 threads/SM)", "fp32x2 (1024 threads/SM)"
 # captures of dram__bytes_read.sum + dram__bytes_write.sum, keyed by
 # (workload, N, threads, ipt, pair-loop variant): the traffic is reported only
 # for the shape that was timed, else null.
-NCU_TRAFFIC = {}
+# N = 2^20 R^3 (cfg1), one launch each (-s 1 -c 1, after the warm-up launch):
+# about 110 MB read (particles, tiles) and 1.6 GB written (the FP64 partial
+# sums of 64 j chunks per i particle).
+NCU_TRAFFIC = {("cfg1", 1 << 20, 128, 2, 1): 110.01e6 + 1.60e9,
+               ("cfg1", 1 << 20, 128, 2, 4): 111.90e6 + 1.60e9,
+               ("cfg1", 1 << 20, 256, 1, 2): 107.21e6 + 1.59e9}
 
 
 def parse():
