@@ -23,9 +23,11 @@ shape, in its FP32 and FP64 builds, on one full wave of i particles against a
 j subset sized to about --ref-seconds per launch.
 
 The default run (cfg1 at one GPU) also measures every other workload in a
-`configs` block of the same JSON line -- cfg0, cfg2 with the image sum and
-with the (rho, z) table at orders 0/2/4, cfg3 at orders 2/4 and on the
-IS_PERIODIC = 3 table (Ng = 127), cfg4 graph against plain launches -- each
+`configs` block of the same JSON line -- cfg0 (one force evaluation per
+step, and as specified: one force + 4 KDK steps, mixed and FP64), cfg2 with
+the image sum and with the (rho, z) table at orders 0/2/4, cfg3 at orders 2/4
+and on the IS_PERIODIC = 3 table (Ng = 127), cfg4 as one persistent kernel
+against a per-phase graph and plain launches -- each
 with its pair rate, issue-roofline fraction, FP64 rate, p50/p99/max against
 FP64 and a short CPU baseline; and a `ref_gpu` block timing the reference's
 own CUDA kernels (FP32 and FP64 builds) on the R^3, T^3 and S1xR2 workloads.
@@ -585,6 +587,63 @@ def run_ours(args, ws, rank, local, dist):
     return line, ps, p, host_table(table, eng), eng, (f32_peak, f64_peak)
 
 
+def kdk_measure(eng, S, W, ps, steps, warmup, f32_peak, nkdk=4, dt=1e-3):
+    """The N = 32,768 workload as specified: one force evaluation, then
+    `nkdk` KDK steps at fixed dt from rest (steps_gpu_forces_resident +
+    steps_gpu_kdk), in mixed precision and in FP64. A step is the whole
+    sequence, CUDA events around it; the uploads of the start state are
+    outside. Mixed R^3 KDK steps rebuild the tiles in the previous Morton
+    order between re-sorts."""
+    import math
+
+    n = ps.n
+    p = S.params(S.R3)
+    rho_part = float(ps.m.min()) / (4.0 * math.pi * W.PARTICLE_RADII ** 3 / 3.0)
+    zeros = np.zeros_like(ps.x)
+    eng.set_particles(ps.m, ps.eps)
+    eng.upload_positions(ps.x)
+    t_tune = time.perf_counter()
+    shape = eng.autotune(p)
+    t_tune = time.perf_counter() - t_tune
+    res = {}
+    for name, prec in (("mixed", S.MIXED), ("fp64", S.FP64)):
+        ms = []
+        for it in range(warmup + steps):
+            eng.upload_positions(ps.x)
+            eng.upload_velocities(zeros)
+            eng.mark(0)
+            eng.forces_resident(p, prec)
+            eng.kdk(p, prec, nkdk, dt, rho_part=rho_part)
+            eng.mark(1)
+            if it >= warmup:
+                ms.append(eng.elapsed_ms(0, 1))
+        res[name] = {"ms_per_step": float(np.mean(ms)), "x": eng.state()[0], "F": eng.state()[2]}
+    pairs = (nkdk + 1) * float(n) * float(n)
+    x, F = res["mixed"]["x"], res["mixed"]["F"]
+    fs = min(2048, n)
+    lo = n // 2 - fs // 2
+    eng.upload_positions(x)
+    eng.forces_resident(p, S.FP64, lo, lo + fs - 1)
+    F64 = eng.download_forces(fs)
+    rel = np.linalg.norm(F[lo:lo + fs] - F64, axis=1) / np.linalg.norm(F64, axis=1)
+    value = pairs / (res["mixed"]["ms_per_step"] * 1e-3)
+    f64_value = pairs / (res["fp64"]["ms_per_step"] * 1e-3)
+    return {"workload": f"R3 compactified N={n} R_max=480 Mpc: one force evaluation + {nkdk} KDK steps at dt={dt} "
+                        f"from rest (the workload as specified), mixed and FP64",
+            "value": value, "unit": UNIT, "ms_per_step": res["mixed"]["ms_per_step"], "steps": steps,
+            "pairs_per_step": pairs, "kernel_shape": shape_desc(shape, argparse.Namespace(shape="", variant=-1)),
+            "autotune_s": t_tune,
+            "roofline": {"bound": "fp32", "frac_of_step": value * 20 / f32_peak, "peak": f32_peak / 1e12,
+                         "flops_per_pair": 20,
+                         "note": "whole step (ordering, tiling, kicks and drifts included) over the FP32 peak"},
+            "fp64": {"pairs_per_s": f64_value, "ms_per_step": res["fp64"]["ms_per_step"]},
+            "speedup_vs_fp64": value / f64_value,
+            "accuracy_mixed_vs_fp64": {"p50": float(np.percentile(rel, 50)), "p99": float(np.percentile(rel, 99)),
+                                       "max": float(rel.max()),
+                                       "sample": f"{fs} i particles: final mixed forces vs the FP64 kernel at the "
+                                                 f"final positions"}}
+
+
 def batch_measure(eng, S, sets, steps, warmup, f32_peak, plain_steps=1):
     """Workload 4: independent compactified R^3 realisations; one force
     evaluation + 10 fixed-dt KDK steps as one persistent kernel under a CUDA
@@ -730,6 +789,10 @@ def run_configs(args, eng, peaks, local):
                      "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                                       "sample": f"{ni} i particles x all {ps.n} j ({dt:.1f} s)"},
                      "wall_s": time.perf_counter() - t0}
+    t0 = time.perf_counter()
+    eng.set_variant(0)
+    out["cfg0_kdk"] = kdk_measure(eng, S, W, W.workload("cfg0"), 3, 1, f32_peak)
+    out["cfg0_kdk"]["wall_s"] = time.perf_counter() - t0
     t0 = time.perf_counter()
     sets = W.r3_ensemble(64)
     r = batch_measure(eng, S, sets, 2, 1, f32_peak)

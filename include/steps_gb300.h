@@ -48,6 +48,7 @@ extern "C" {
 #define STEPS_E_NOMEM 4   /* device allocation failed */
 #define STEPS_E_TABLE 5   /* table shape does not match the request */
 #define STEPS_E_TIMEOUT 6 /* a bounded device-side wait gave up (status written by the kernel) */
+#define STEPS_E_BOUNDS 7  /* debug build (libsteps_gb300_check.so) only: an index failed its bounds check */
 
 /* Topologies (compile-time PERIODIC / PERIODIC_Z switches in StePS,
  * StePS/Template-LinuxGCC-Makefile:29-32). */
@@ -202,7 +203,10 @@ int steps_gpu_upload_velocities(const double *v);
  * the resident x, v: kick h/2 + drift h, periodic wrap, force, kick h/2, with
  * acceleration g*F*a^-3 - 2*hubble*v. Computes the forces of the current
  * positions first if none are resident. errmax (step.cc:265-269, with
- * rho_part) of the last step is written to *errmax_out when non-NULL. */
+ * rho_part) of the last step is written to *errmax_out when non-NULL.
+ * Mixed-precision R^3 steps re-sort the particles every 8th step and in
+ * between rebuild the tiles in the previous order (same forces, less
+ * preparation); periodic topologies re-sort every step. */
 int steps_gpu_kdk(const steps_params *p, int precision, int nsteps, double h, double g, double a, double hubble,
                   double rho_part, double *errmax_out);
 
@@ -246,7 +250,10 @@ int steps_gpu_set_tuning(int threads, int ipt, int jsplit);
  * with 768 / 1024 resident threads per SM asked of the register allocator,
  * 4 = packed with the j tiles streamed by bulk copies (TMA) through an
  * mbarrier ring (bounded waits; STEPS_E_TIMEOUT if one gives up). Same results
- * to rounding; the autotuner picks among them. */
+ * to rounding; the autotuner picks among them. T^3 with a trilinear table reads
+ * the same setting as 1 = quad lanes (one i per thread; the 4 lanes of a quad take one
+ * i against 4 neighbouring j per step, so table loads share cache lines), any
+ * other value = one i per lane. */
 int steps_gpu_set_kernel_variant(int variant);
 
 /* T^3 mixed precision: capacity, in table cells (16 bytes each), of the
@@ -321,6 +328,19 @@ int steps_gpu_test_stall_copy(long long tile_seq);
  * stage run out after about a second; the call returns STEPS_E_TIMEOUT and the
  * context stays usable. -1 cancels. One shot. */
 int steps_gpu_test_stall_ensemble(int realisation);
+
+/* Debug bounds checks. libsteps_gb300_check.so is the same library built with
+ * -DSTEPS_CHECK: every kernel compares its tile, chunk, slot, output-row,
+ * table-cell and ordering indices with their bounds, records the first one out
+ * of range, keeps the access inside its buffer, and the call returns
+ * STEPS_E_BOUNDS with the site, index and bound in steps_gpu_error_string().
+ * steps_gpu_checks_compiled() is 1 in that build, 0 in the normal one.
+ * steps_gpu_test_bounds_check() checks the mechanism itself: in the checked
+ * build it launches one kernel that submits `index` against the bound 16 (the
+ * index is never dereferenced) and returns STEPS_E_BOUNDS when index is outside
+ * [0, 16), STEPS_OK otherwise; in the normal build it returns STEPS_E_STATE. */
+int steps_gpu_checks_compiled(void);
+int steps_gpu_test_bounds_check(int index);
 
 /* ---- allocation-free entry point ----------------------------------------- */
 

@@ -15,9 +15,13 @@ import numpy as np
 from . import workloads  # noqa: F401
 
 PKG = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(PKG, "_build", "libsteps_gb300.so")
+# STEPS_GB300_LIB selects another in-tree build of the library, e.g. the
+# bounds-checked _build/check/libsteps_gb300_check.so.
+LIB_PATH = os.environ.get("STEPS_GB300_LIB") or os.path.join(PKG, "_build", "libsteps_gb300.so")
+CHECK_LIB_PATH = os.path.join(PKG, "_build", "check", "libsteps_gb300_check.so")
 
-STEPS_OK, STEPS_E_ARG, STEPS_E_STATE, STEPS_E_CUDA, STEPS_E_NOMEM, STEPS_E_TABLE, STEPS_E_TIMEOUT = range(7)
+(STEPS_OK, STEPS_E_ARG, STEPS_E_STATE, STEPS_E_CUDA, STEPS_E_NOMEM, STEPS_E_TABLE, STEPS_E_TIMEOUT,
+ STEPS_E_BOUNDS) = range(8)
 R3, T3, S1R2 = 0, 1, 2
 FP64, MIXED = 0, 1
 
@@ -250,6 +254,14 @@ class Engine:
 
     def test_stall_ensemble(self, realisation: int):
         self._check(self.lib.steps_gpu_test_stall_ensemble(int(realisation)))
+
+    def checks_compiled(self) -> bool:
+        return bool(self.lib.steps_gpu_checks_compiled())
+
+    def test_bounds_check(self, index: int) -> tuple[int, str]:
+        """Status and message of one self-test index against the bound 16."""
+        rc = self.lib.steps_gpu_test_bounds_check(int(index))
+        return rc, self.lib.steps_gpu_error_string().decode() if rc else ""
 
     def batch_get(self, k):
         n = self._batch[k][1].size

@@ -42,6 +42,59 @@ void check_cuda(cudaError_t e, const char *what, const char *file, int line)
 
 void add_launches(long long k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
 
+#ifdef STEPS_CHECK
+static std::vector<void *(*)()> &check_registry()
+{
+    static std::vector<void *(*)()> r;
+    return r;
+}
+
+int register_check_record(void *(*where)())
+{
+    check_registry().push_back(where);
+    return (int)check_registry().size();
+}
+
+static const char *check_site_name(int site)
+{
+    static const char *names[CK_NSITES] = {"none", "i tile", "j tile range", "j chunk", "partial slot",
+                                           "output row", "T3 FP32 table cell", "T3 FP64 table cell",
+                                           "S1xR2 table cell", "radial table entry", "particle index",
+                                           "radix-sort destination", "self-test index"};
+    return site >= 0 && site < CK_NSITES ? names[site] : "unknown site";
+}
+
+// Reads the bounds-check record of every translation unit after a call; the
+// first one set fails the call with STEPS_E_BOUNDS and is cleared.
+static void check_bounds_records()
+{
+    if (g_ctx.device < 0) return;
+    STEPS_CUDA(cudaDeviceSynchronize());
+    for (auto where : check_registry()) {
+        void *p = where();
+        if (!p) continue;
+        CheckRecord r;
+        STEPS_CUDA(cudaMemcpy(&r, p, sizeof r, cudaMemcpyDeviceToHost));
+        if (r.code == 0) continue;
+        const CheckRecord none{};
+        STEPS_CUDA(cudaMemcpy(p, &none, sizeof none, cudaMemcpyHostToDevice));
+        g_ctx.F_ni = 0;
+        g_ctx.F_valid = false;
+        char buf[200];
+        snprintf(buf, sizeof buf, "bounds check failed: %s %lld outside [0, %lld)", check_site_name(r.site), r.index,
+                 r.bound);
+        fail(STEPS_E_BOUNDS, buf);
+    }
+}
+#endif
+
+__global__ void k_check_selftest(int index)
+{
+    int v = index;
+    STEPS_CHECK_IDX(v, 16, CK_SELFTEST);
+    (void)v;
+}
+
 void note_launch(const char *name)
 {
     g_launches.fetch_add(1, std::memory_order_relaxed);
@@ -212,6 +265,9 @@ static int guarded(Fn &&fn)
 {
     try {
         fn();
+#ifdef STEPS_CHECK
+        check_bounds_records();
+#endif
         return STEPS_OK;
     } catch (const Error &e) {
         g_err = e.msg;
@@ -234,6 +290,27 @@ extern "C" {
 int steps_gpu_abi_version(void) { return STEPS_GB300_ABI_VERSION; }
 
 const char *steps_gpu_error_string(void) { return g_err.c_str(); }
+
+int steps_gpu_checks_compiled(void)
+{
+#ifdef STEPS_CHECK
+    return 1;
+#else
+    return 0;
+#endif
+}
+
+int steps_gpu_test_bounds_check(int index)
+{
+    return guarded([&] {
+        require_init();
+#ifndef STEPS_CHECK
+        fail(STEPS_E_STATE, "bounds checks are compiled into libsteps_gb300_check.so only");
+#endif
+        k_check_selftest<<<1, 1, 0, g_ctx.stream>>>(index);
+        note_launch("k_check_selftest");
+    });
+}
 
 int steps_gpu_init(int device)
 {
@@ -489,8 +566,11 @@ int steps_gpu_autotune(const steps_params *p, int id_min, int id_max, int *out)
         Shape keep = c.shape;
         Shape bestS = keep;
         KParams kp = derive_params(p);
-        // R^3: the scalar and packed pair loops as well.
-        const int nvar = kp.topology == STEPS_R3 ? R3_VARIANTS : 1;
+        // R^3: the scalar and packed pair loops as well; T^3 with a table: the
+        // one-i-per-lane and quad-lane kernels.
+        const int nvar = kp.topology == STEPS_R3                          ? R3_VARIANTS
+                         : kp.topology == STEPS_T3 && kp.is_periodic >= 2 ? T3_VARIANTS
+                                                                          : 1;
         // Stage 1: each candidate is scored by its time per pair on a strided
         // sample of the real i tiles, 24 waves of items (one untimed launch,
         // one timed; the whole range if it is smaller). Fewer waves misrank
@@ -525,8 +605,10 @@ int steps_gpu_autotune(const steps_params *p, int id_min, int id_max, int *out)
         for (int v = 0; v < nvar; v++)
             for (auto &s : shapes) {
                 if (!shape_supported_for(kp, s[0], s[1])) continue;
-                if (v >= 1 && v <= 3 && !r3x2_kernel(s[0], s[1], false, r3x2_occ(v))) continue;
-                if (v == 4 && !r3x2_pipe_kernel(s[0], s[1])) continue;
+                if (kp.topology == STEPS_R3 && v >= 1 && v <= 3 && !r3x2_kernel(s[0], s[1], false, r3x2_occ(v)))
+                    continue;
+                if (kp.topology == STEPS_R3 && v == 4 && !r3x2_pipe_kernel(s[0], s[1])) continue;
+                if (kp.topology == STEPS_T3 && v == 1 && !t3_quad_kernel(kp, s[0], s[1])) continue;
                 Shape sh = keep;
                 sh.threads = s[0];
                 sh.ipt = s[1];
@@ -569,7 +651,7 @@ int steps_gpu_set_kernel_variant(int variant)
     return guarded([&] {
         if (variant < 0 || variant >= R3_VARIANTS)
             fail(STEPS_E_ARG, "kernel variant must be 0 (scalar), 1 (packed FP32x2), 2 or 3 (packed, 768 or 1024 "
-                              "threads per SM) or 4 (packed, bulk-copy pipeline)");
+                              "threads per SM) or 4 (packed, bulk-copy pipeline); for T3, 1 selects quad lanes");
         g_ctx.shape.variant = variant;
     });
 }

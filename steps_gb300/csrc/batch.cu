@@ -110,17 +110,22 @@ __global__ void k_batch_keys(const double *__restrict__ x, const uint16_t *__res
 
 // Sum each i's slots in order and scatter to caller order.
 __global__ void k_batch_reduce(const double *__restrict__ part, const int2 *__restrict__ tslot,
-                               const uint32_t *__restrict__ idx, int npad, int T, double *__restrict__ F)
+                               const uint32_t *__restrict__ idx, int npad, int T, int n, int nslots,
+                               double *__restrict__ F)
 {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= npad) return;
-    const uint32_t o = idx[q];
+    uint32_t o = idx[q];
     if (o == PAD_J) return;
+    STEPS_CHECK_IDX(o, n, CK_OUTPUT);
     const int t = q / T, e = q - t * T;
     const int2 s = tslot[t];
     double f[3] = {0, 0, 0};
-    for (int k = 0; k < s.y; k++)
-        for (int c = 0; c < 3; c++) f[c] += part[((size_t)(s.x + k) * T + e) * 3 + c];
+    for (int k = 0; k < s.y; k++) {
+        int slot = s.x + k;
+        STEPS_CHECK_IDX(slot, nslots, CK_SLOT);
+        for (int c = 0; c < 3; c++) f[c] += part[((size_t)slot * T + e) * 3 + c];
+    }
     for (int c = 0; c < 3; c++) F[3 * (size_t)o + c] = f[c];
 }
 
@@ -248,6 +253,7 @@ void batch_forces(Batch &b)
     a.njt = a.nit = b.ntiles;
     a.nitems = b.nitems;
     a.items = b.items.as<int4>();
+    a.nslots = b.nitems;
     a.counter = b.counter.as<unsigned>();
     a.part = b.part.as<double>();
     a.guard2 = c.shape.guard * c.shape.guard;
@@ -256,8 +262,8 @@ void batch_forces(Batch &b)
     fn<<<b.grid, b.threads, 0, st>>>(a);
     note_launch("k_pair_r3x2(list)");
     k_batch_reduce<<<div_up(b.ntiles * b.T, 256), 256, 0, st>>>(b.part.as<double>(), b.tslot.as<int2>(),
-                                                                b.ts.idx.as<uint32_t>(), b.ntiles * b.T, b.T,
-                                                                b.F.as<double>());
+                                                                b.ts.idx.as<uint32_t>(), b.ntiles * b.T, b.T, b.ntot,
+                                                                b.nitems, b.F.as<double>());
     note_launch("k_batch_reduce");
 }
 
@@ -308,6 +314,10 @@ void ensemble_run(Batch &b, int nsteps, double h, int stall_rel)
     e.guard2 = c.shape.guard * c.shape.guard;
     e.status = kernel_status_word();
     e.stall_rel = stall_rel;
+    e.ntiles = b.ntiles;
+    e.nslots = b.nitems;
+    e.nrel = b.count;
+    e.n = b.ntot;
     mixed::EnsembleFn fn = ensemble_kernel(b.threads, b.ipt);
     if (!fn) fail(STEPS_E_ARG, "batch: unsupported kernel shape");
     fn<<<b.ens_grid, b.threads, 0, st>>>(e);

@@ -105,6 +105,84 @@ void note_launch(const char *name);
 // Adds kernels launched by other means (the kernel nodes of a graph launch).
 void add_launches(long long k);
 
+// ------------------------------------------------- debug bounds checks --
+//
+// Compiled with -DSTEPS_CHECK (libsteps_gb300_check.so), STEPS_CHECK_IDX(v,
+// bound, site) compares the index variable v with [0, bound). The first index
+// out of range in this translation unit is recorded (site, index, bound), v
+// is set to 0 so that the access it guards stays inside its buffer, and the
+// C-ABI call that launched the kernel returns STEPS_E_BOUNDS with the record
+// in its message. In the normal build the macro is empty.
+enum CheckSite {
+    CK_NONE = 0,
+    CK_I_TILE,      // i tile of a work item
+    CK_J_TILE,      // j tile range of a work item
+    CK_CHUNK,       // j chunk (partial slab) of a work item
+    CK_SLOT,        // partial slot of a work-list item or of an i tile
+    CK_OUTPUT,      // caller-order output row (curve position -> original index - id_min)
+    CK_T3_CELL,     // cell of the FP32 T^3 table (haloed copy, window or wrapped read)
+    CK_T3_FP64,     // cell of the FP64 T^3 table
+    CK_S1_CELL,     // (rho, z) cell of the S1xR2 table or of its records
+    CK_RADIAL,      // entry of the cylindrical radial-force table
+    CK_PERM,        // original particle index read from the ordering
+    CK_SCATTER,     // destination of a radix-sort scatter
+    CK_SELFTEST,    // steps_gpu_test_bounds_check
+    CK_NSITES
+};
+
+struct CheckRecord {
+    int code;  // 0, or STEPS_E_BOUNDS once an index failed
+    int site;
+    long long index, bound;
+};
+
+#ifdef STEPS_CHECK
+static __device__ CheckRecord g_check_record;
+
+static __device__ __noinline__ void check_failed(long long index, long long bound, int site)
+{
+    if (atomicCAS(&g_check_record.code, 0, STEPS_E_BOUNDS) == 0) {
+        g_check_record.site = site;
+        g_check_record.index = index;
+        g_check_record.bound = bound;
+        __threadfence();
+    }
+}
+
+#define STEPS_CHECK_IDX(v, bound, site)                                                          \
+    do {                                                                                         \
+        if ((unsigned long long)(long long)(v) >= (unsigned long long)(long long)(bound)) {     \
+            ::steps::check_failed((long long)(v), (long long)(bound), (site));                   \
+            (v) = 0;                                                                             \
+        }                                                                                        \
+    } while (0)
+
+// True when the cells [first, last] lie in [0, bound); otherwise records the
+// offending end and returns false (the caller then moves the access to 0).
+static __device__ __forceinline__ bool check_span(long long first, long long last, long long bound, int site)
+{
+    if (first >= 0 && last < bound) return true;
+    check_failed(first < 0 ? first : last, bound, site);
+    return false;
+}
+
+// Each translation unit registers where its record lives; the C-ABI reads
+// every record after each call.
+int register_check_record(void *(*where)());
+static void *check_record_address()
+{
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_check_record) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return p;
+}
+static const int g_check_registered = register_check_record(&check_record_address);
+#else
+#define STEPS_CHECK_IDX(v, bound, site) ((void)0)
+#endif
+
 // ---------------------------------------------------- device math helpers --
 
 // Order-preserving integer image of a double (atomic min/max of bounding boxes).

@@ -135,6 +135,7 @@ __device__ __forceinline__ void add_background(const Background &bg, const doubl
         int i = (int)floor(r / bg.rsim * (sz - 1));
         double c = bg.radial[sz - 1];
         if (i < sz - 1) {
+            STEPS_CHECK_IDX(i, sz - 1, CK_RADIAL);
             double x1 = step * i, y1 = bg.radial[i], x2 = step * (i + 1), y2 = bg.radial[i + 1];
             double A = (y2 - y1) / (x2 - x1);
             double B = y1 - A * x1;

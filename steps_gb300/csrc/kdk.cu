@@ -79,6 +79,16 @@ double kdk_kick_err(double *v, const double *F, const double *m, int n, double h
 
 using namespace steps;
 
+// Mixed R^3 steps keep the Morton order of the last sort for
+// KDK_RESORT_EVERY - 1 steps and only rebuild the tiles (centres, extents,
+// offsets, sub-tile boxes) from the drifted positions: one leapfrog step moves
+// a particle a small fraction of its tile, the forces do not depend on the
+// order (a looser tile only sends more tile pairs down the exact near path),
+// and the sort is most of the preparation at small N. Periodic topologies
+// re-sort every step: a particle wrapped across the box would stretch its
+// tile over the whole period.
+static constexpr int KDK_RESORT_EVERY = 8;
+
 extern "C" int steps_gpu_kdk(const steps_params *p, int precision, int nsteps, double h, double g, double a,
                              double hubble, double rho_part, double *errmax_out)
 {
@@ -105,7 +115,8 @@ extern "C" int steps_gpu_kdk(const steps_params *p, int precision, int nsteps, d
             for (int s = 0; s < q.nsteps; s++) {
                 kdk_kick_drift(c.x.as<double>(), c.v.as<double>(), c.F.as<double>(), c.n, q.h, q.g, a3, q.hubble,
                                wrap, q.p->L, c.stream);
-                compute_forces(q.p, q.precision, 0, c.n - 1, false);
+                const bool reuse = q.p->topology == STEPS_R3 && (s + 1) % KDK_RESORT_EVERY != 0;
+                compute_forces(q.p, q.precision, 0, c.n - 1, reuse);
                 e = kdk_kick_err(c.v.as<double>(), c.F.as<double>(), c.m64.as<double>(), c.n, q.h, q.g, a3, q.hubble,
                                  q.rho_part, es, c.stream, s == q.nsteps - 1);
             }

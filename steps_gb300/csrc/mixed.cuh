@@ -31,6 +31,7 @@ struct MixedArgs {
     int *status;        // STEPS_E_TIMEOUT written here by a pipeline wait that gave up
     long long stall_seq;  // test hook: block 0 withholds the copy of its tile number stall_seq (-1: none)
     const int4 *items;  // work list (batches): i tile, j tile begin, j tile end, partial slot
+    int nslots;         // partial slots of the work list (bounds checks)
     double *part;       // [S][nit*T][3]
     size_t part_stride; // nit*T*3
     float L, halfL, cutL;
@@ -74,6 +75,7 @@ __device__ __forceinline__ void stage_tile(const MixedArgs &a, int J, float4 *sp
                                            float4 *sres)
 {
     constexpr int T = BLOCK * IPT;
+    STEPS_CHECK_IDX(J, a.njt, CK_J_TILE);
 #pragma unroll
     for (int k = 0; k < IPT; k++) {
         int e = k * BLOCK + threadIdx.x;
@@ -359,6 +361,7 @@ struct EnsembleArgs {
     float guard2;
     int *status;            // STEPS_E_TIMEOUT when a stage wait gave up
     int stall_rel;          // test hook: this realisation's stage-0 tiles are never reported done (-1: none)
+    int ntiles, nslots, nrel, n;  // tiles, partial slots, realisations, particles (bounds checks)
 };
 using EnsembleFn = void (*)(EnsembleArgs);
 
@@ -366,7 +369,12 @@ using EnsembleFn = void (*)(EnsembleArgs);
 
 // pair_t3.cu: T^3 kernel for a shape (dynamic shared memory returned) and its
 // table arguments (FP32 table copy, grid geometry).
-mixed::KernelFn t3_kernel(const KParams &kp, int threads, int ipt, size_t *dyn_smem);
+// variant 0: one i per lane (optionally with the shared-memory window);
+// variant 1: quad lanes where t3_quad_kernel has them (trilinear, one i per
+// thread), else as 0.
+mixed::KernelFn t3_kernel(const KParams &kp, int threads, int ipt, size_t *dyn_smem, int variant = 0);
+mixed::KernelFn t3_quad_kernel(const KParams &kp, int threads, int ipt);
+constexpr int T3_VARIANTS = 2;
 void t3_args(mixed::MixedArgs &a, const KParams &kp, const Tables &tb, cudaStream_t st);
 // pair_r3x2.cu: R^3 kernel on packed FP32 pairs; occ = 0, 768 or 1024
 // resident threads per SM requested from the register allocator.

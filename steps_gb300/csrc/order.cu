@@ -147,6 +147,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_scatter(const unsigned long lo
         __syncthreads();
         if (valid) {
             uint32_t pos = wc[w][d] + rank;
+            STEPS_CHECK_IDX(pos, n, CK_SCATTER);
             kout[pos] = key;
             vout[pos] = val;
         }
@@ -161,7 +162,8 @@ constexpr int TB_THREADS = 256;
 // start and count.
 __global__ void __launch_bounds__(TB_THREADS) k_tile_build(const double *__restrict__ x, const double *__restrict__ m,
                                                           const double *__restrict__ eps,
-                                                          const uint32_t *__restrict__ perm, int count, int T,
+                                                          const uint32_t *__restrict__ perm, long long nx,
+                                                          int count, int T,
                                                           float4 *__restrict__ pack, float *__restrict__ epsf,
                                                           float4 *__restrict__ meta, uint32_t *__restrict__ idx,
                                                           uint32_t pad_id, float4 *__restrict__ lo,
@@ -170,8 +172,12 @@ __global__ void __launch_bounds__(TB_THREADS) k_tile_build(const double *__restr
 {
     const int tile = blockIdx.x;
     const int sbase = tdesc ? tdesc[tile].x : tile * T;
-    const int cnt = tdesc ? tdesc[tile].y : min(T, count - tile * T);
-    build_tile<TB_THREADS, false>(tile, sbase, cnt, x, m, eps, perm, T, pack, epsf, meta, idx, pad_id, lo, soa, sub);
+    int cnt = tdesc ? tdesc[tile].y : min(T, count - tile * T);
+#ifdef STEPS_CHECK
+    if (!check_span(sbase, (long long)sbase + cnt - 1, count, CK_PERM)) cnt = 0;
+#endif
+    build_tile<TB_THREADS, false>(tile, sbase, cnt, x, m, eps, perm, nx, T, pack, epsf, meta, idx, pad_id, lo, soa,
+                                  sub);
 }
 
 }  // namespace
@@ -242,7 +248,8 @@ void build_tiles(TileSet &ts, const double *x, const double *m64, const double *
     ts.resid.ensure<float4>(padded);
     ts.soa.ensure<float4>(padded);
     ts.sub.ensure<float4>(2 * (padded / SUBTILE));
-    k_tile_build<<<ts.ntiles, TB_THREADS, 0, st>>>(x, m64, eps64, ts.perm(), count, T, ts.pack.as<float4>(),
+    k_tile_build<<<ts.ntiles, TB_THREADS, 0, st>>>(x, m64, eps64, ts.perm(), (long long)lo + count, count, T,
+                                                   ts.pack.as<float4>(),
                                                    ts.eps.as<float>(), ts.meta.as<float4>(), ts.idx.as<uint32_t>(),
                                                    pad_id, ts.resid.as<float4>(), ts.soa.as<float>(), nullptr,
                                                    ts.sub.as<float4>());
@@ -268,8 +275,8 @@ void tile_build_range(const double *x, const double *m64, const double *eps64, c
                       const int2 *tdesc, int ntiles, cudaStream_t st, float4 *sub)
 {
     int nt = tdesc ? ntiles : div_up(count, T);
-    k_tile_build<<<nt, TB_THREADS, 0, st>>>(x, m64, eps64, perm, count, T, pack, epsf, meta, idx, pad_id, lo, soa,
-                                            tdesc, sub);
+    k_tile_build<<<nt, TB_THREADS, 0, st>>>(x, m64, eps64, perm, count, count, T, pack, epsf, meta, idx, pad_id, lo,
+                                            soa, tdesc, sub);
     note_launch("k_tile_build");
 }
 

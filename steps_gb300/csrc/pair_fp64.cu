@@ -55,14 +55,17 @@ __device__ __forceinline__ void t3_interp_fp64(const double *__restrict__ tab, i
 #pragma unroll
     for (int a = 0; a < ORDER; a++) {
         int ix = pos_mod(i0[0] + OFF + a, ng);
+        STEPS_CHECK_IDX(ix, ng, CK_T3_FP64);
 #pragma unroll
         for (int b = 0; b < ORDER; b++) {
             int iy = pos_mod(i0[1] + OFF + b, ng);
+            STEPS_CHECK_IDX(iy, ng, CK_T3_FP64);
             double wxy = w[0][a] * w[1][b];
             const double *row = tab + (size_t)(ix * ng + iy) * ng * 3;
 #pragma unroll
             for (int c = 0; c < ORDER; c++) {
                 int iz = pos_mod(i0[2] + OFF + c, ng);
+                STEPS_CHECK_IDX(iz, ng, CK_T3_FP64);
                 double ww = wxy * w[2][c];
                 s0 += ww * __ldg(row + 3 * iz);
                 s1 += ww * __ldg(row + 3 * iz + 1);
@@ -90,7 +93,11 @@ __device__ __forceinline__ void s1r2_interp_fp64(const double *__restrict__ T, i
     double ur = drho > 0 ? rr / drho : 0.0;
     double uz = (dz + half) / dzc - 0.5;
     double Dr = 0, Dzz = 0;
-    auto at = [&](int ir, int iz, int c) { return __ldg(T + ((size_t)ir * nz + iz) * 2 + c); };
+    auto at = [&](int ir, int iz, int c) {
+        STEPS_CHECK_IDX(ir, nrho, CK_S1_CELL);
+        STEPS_CHECK_IDX(iz, nz, CK_S1_CELL);
+        return __ldg(T + ((size_t)ir * nz + iz) * 2 + c);
+    };
     if (ORDER == 0) {
         int ir = (int)floor(ur + 0.5);
         int iz = (int)floor(uz + 0.5);

@@ -52,7 +52,8 @@ __global__ void __launch_bounds__(BLOCK, KIND == K_R3 && IPT == 1 ? 1024 / BLOCK
         __syncthreads();
         const int item = s_item;
         if (item >= a.nitems) return;
-        const int I = (item / a.S) * a.istride;
+        int I = (item / a.S) * a.istride;
+        STEPS_CHECK_IDX(I, a.nit, CK_I_TILE);
         const int chunk = item % a.S;
         const int J0 = chunk * a.tpc;
         const int J1 = min(a.njt, J0 + a.tpc);
@@ -397,8 +398,11 @@ __global__ void k_reduce_mixed(const double *__restrict__ part, int S, size_t st
     for (int s = 0; s < S; s++)
         for (int k = 0; k < 3; k++) f[k] += part[(size_t)s * stride + 3 * (size_t)q + k];
     uint32_t o = perm[q];
+    long long row = (long long)o - id_min;
+    STEPS_CHECK_IDX(row, count, CK_OUTPUT);
+    o = (uint32_t)(row + id_min);
     add_background(bg, x + 3 * (size_t)o, f);
-    for (int k = 0; k < 3; k++) F[3 * (size_t)(o - id_min) + k] = f[k];
+    for (int k = 0; k < 3; k++) F[3 * (size_t)row + k] = f[k];
 }
 
 template <int KIND, int EMAX>
@@ -459,7 +463,9 @@ void forces_mixed(const KParams &kp, const Tables &tb, const double *x, const do
     size_t dyn = 0;
     const bool s1tab = kp.topology == STEPS_S1R2 && kp.is_periodic >= 2 && !kp.s1r2_images;
     const bool packed = kp.topology == STEPS_R3 && c.shape.variant >= 1;
-    KernelFn fn = kp.topology == STEPS_T3 ? t3_kernel(kp, threads, ipt, &dyn)
+    // T^3 reads the variant as 0 (one i per lane) or 1 (quad lanes); the R^3
+    // pair loops 2-4 have no T^3 counterpart and mean 0 there.
+    KernelFn fn = kp.topology == STEPS_T3 ? t3_kernel(kp, threads, ipt, &dyn, c.shape.variant == 1 ? 1 : 0)
                   : s1tab              ? s1tab_kernel(kp, threads, ipt)
                   : packed             ? (c.shape.variant == 4 ? r3x2_pipe_kernel(threads, ipt)
                                                                : r3x2_kernel(threads, ipt, false, r3x2_occ(c.shape.variant)))

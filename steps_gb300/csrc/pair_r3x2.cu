@@ -29,6 +29,7 @@ __device__ __forceinline__ void stage_soa(const MixedArgs &a, int J, float *sx, 
 {
     constexpr int T = BLOCK * IPT;
     constexpr int NS2 = 2 * (T / SUBTILE);  // float4 of sub-tile boxes per tile
+    STEPS_CHECK_IDX(J, a.njt, CK_J_TILE);
     const float4 *src = reinterpret_cast<const float4 *>(a.jsoa + (size_t)J * 4 * T);
     float4 *dst = reinterpret_cast<float4 *>(sx);
     for (int e = threadIdx.x; e < NS2; e += BLOCK) cp_async16(ssub + e, a.jsub + (size_t)J * NS2 + e);
@@ -221,12 +222,16 @@ __device__ __forceinline__ void r3x2_body(const MixedArgs &a)
             I = d.x;
             J0 = d.y;
             J1 = d.z;
-            base = (size_t)d.w * 3 * T;
+            int slot = d.w;
+            STEPS_CHECK_IDX(slot, a.nslots, CK_SLOT);
+            STEPS_CHECK_IDX(I, a.nit, CK_I_TILE);
+            base = (size_t)slot * 3 * T;
         } else {
             I = (item / a.S) * a.istride;
             const int chunk = item % a.S;
             J0 = chunk * a.tpc;
             J1 = min(a.njt, J0 + a.tpc);
+            STEPS_CHECK_IDX(I, a.nit, CK_I_TILE);
             base = (size_t)chunk * a.part_stride + 3 * (size_t)I * T;
         }
 
@@ -320,6 +325,7 @@ __device__ __forceinline__ void r3x2_pipe_body(const MixedArgs &a)
     unsigned long long issued = 0;    // tiles whose copy thread 0 has issued
     unsigned long long consumed = 0;  // tiles this thread's warp has finished (the same in every warp)
     auto issue = [&](int J) -> bool {  // thread 0
+        STEPS_CHECK_IDX(J, a.njt, CK_J_TILE);
         const int st = (int)(issued % S);
         if (issued >= S && !mbar_wait(&empty[st], (unsigned)((issued / S - 1) & 1))) return false;
         mbar_arrive_expect_tx(&full[st], BYTES);
@@ -345,7 +351,8 @@ __device__ __forceinline__ void r3x2_pipe_body(const MixedArgs &a)
         __syncthreads();
         const int item = s_item;
         if (item >= a.nitems) break;
-        const int I = (item / a.S) * a.istride;
+        int I = (item / a.S) * a.istride;
+        STEPS_CHECK_IDX(I, a.nit, CK_I_TILE);
         const int chunk = item % a.S;
         const int J0 = chunk * a.tpc;
         const int J1 = min(a.njt, J0 + a.tpc);
@@ -474,11 +481,14 @@ __device__ __forceinline__ void ensemble_finish_tile(const EnsembleArgs &e, int 
     const bool kick2 = stage >= 1, kick1 = stage < e.nstages - 1;
     const double h2 = e.h / 2.0;
     for (int p = tid; p < T; p += BLOCK) {
-        const uint32_t o = __ldg(e.jidx + (size_t)I * T + p);
+        uint32_t o = __ldg(e.jidx + (size_t)I * T + p);
         if (o == 0xffffffffu) continue;  // padding
+        STEPS_CHECK_IDX(o, e.n, CK_PERM);
         double f[3] = {0.0, 0.0, 0.0};
         for (int s = 0; s < sl.y; s++) {
-            const double *pc = e.part + ((size_t)(sl.x + s) * T + p) * 3;
+            int slot = sl.x + s;
+            STEPS_CHECK_IDX(slot, e.nslots, CK_SLOT);
+            const double *pc = e.part + ((size_t)slot * T + p) * 3;
             f[0] += __ldcg(pc);
             f[1] += __ldcg(pc + 1);
             f[2] += __ldcg(pc + 2);
@@ -499,13 +509,14 @@ __device__ __forceinline__ void ensemble_finish_tile(const EnsembleArgs &e, int 
     __syncthreads();
     if (kick1) {
         const int nb = (stage + 1) & 1;
-        build_tile<BLOCK, true>(I, td.x, td.y, e.x, e.m64, e.eps64, e.perm, T, e.pack_w[nb], e.epsf_w, e.meta_w[nb],
+        build_tile<BLOCK, true>(I, td.x, td.y, e.x, e.m64, e.eps64, e.perm, e.n, T, e.pack_w[nb], e.epsf_w, e.meta_w[nb],
                                 nullptr, 0xffffffffu, e.resid_w[nb], e.soa_w[nb], e.sub_w[nb]);
     }
     __syncthreads();
     if (tid == 0) {
         __threadfence();
-        const int k = __ldg(e.tile_rel + I);
+        int k = __ldg(e.tile_rel + I);
+        STEPS_CHECK_IDX(k, e.nrel, CK_I_TILE);
         if (!(stage == 0 && k == e.stall_rel)) atomicAdd(e.rel_done + k, 1u);
     }
 }
@@ -536,7 +547,10 @@ __global__ void __launch_bounds__(BLOCK, BLOCK <= 128 && IPT <= 2 ? 640 / BLOCK 
             int task = *st != 0 ? ntasks : (int)atomicAdd(e.queue, 1u);
             if (task < ntasks && task >= e.nitems) {  // stage >= 1: wait for the previous stage of this realisation
                 const int stage = task / e.nitems;
-                const int k = __ldg(e.tile_rel + __ldg(e.items + task % e.nitems).x);
+                int it = __ldg(e.items + task % e.nitems).x;
+                STEPS_CHECK_IDX(it, e.ntiles, CK_I_TILE);
+                int k = __ldg(e.tile_rel + it);
+                STEPS_CHECK_IDX(k, e.nrel, CK_I_TILE);
                 if (!wait_counter(e.rel_done + k, (unsigned)(__ldg(e.rel_ntiles + k) * stage), e.status)) {
                     atomicExch(e.status, STEPS_E_TIMEOUT);
                     task = ntasks;
@@ -551,7 +565,10 @@ __global__ void __launch_bounds__(BLOCK, BLOCK <= 128 && IPT <= 2 ? 640 / BLOCK 
         const int stage = task / e.nitems;
         const int b = stage & 1;
         const int4 d = __ldg(e.items + task % e.nitems);
-        const int I = d.x, J0 = d.y, J1 = d.z;
+        int I = d.x, slot = d.w;
+        const int J0 = d.y, J1 = d.z;
+        STEPS_CHECK_IDX(I, e.ntiles, CK_I_TILE);
+        STEPS_CHECK_IDX(slot, e.nslots, CK_SLOT);
         const float4 *ipack = e.pack[b], *ilo = e.resid[b], *imeta = e.meta[b];
 
         const float4 mI0 = __ldcg(imeta + 2 * I);
@@ -578,6 +595,7 @@ __global__ void __launch_bounds__(BLOCK, BLOCK <= 128 && IPT <= 2 ? 640 / BLOCK 
         const float wemax = warp_eps_max<IPT>(ei);
 
         MixedArgs a;  // the fields stage_soa reads
+        a.njt = e.ntiles;
         a.jsoa = e.soa[b];
         a.jeps = e.jeps;
         a.jidx = e.jidx;
@@ -598,7 +616,7 @@ __global__ void __launch_bounds__(BLOCK, BLOCK <= 128 && IPT <= 2 ? 640 / BLOCK 
             __syncthreads();
         }
 
-        double *o = e.part + (size_t)d.w * 3 * T;
+        double *o = e.part + (size_t)slot * 3 * T;
 #pragma unroll
         for (int k = 0; k < IPT; k++) {
             const size_t q = k * BLOCK + tid;

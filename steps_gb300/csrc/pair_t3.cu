@@ -132,7 +132,8 @@ __global__ void __launch_bounds__(BLOCK) k_pair_t3(MixedArgs a)
         __syncthreads();
         const int item = s_item;
         if (item >= a.nitems) return;
-        const int I = (item / a.S) * a.istride;
+        int I = (item / a.S) * a.istride;
+        STEPS_CHECK_IDX(I, a.nit, CK_I_TILE);
         const int chunk = item % a.S;
         const int J0 = chunk * a.tpc;
         const int J1 = min(a.njt, J0 + a.tpc);
@@ -221,7 +222,9 @@ __global__ void __launch_bounds__(BLOCK) k_pair_t3(MixedArgs a)
                     const int cy = rem / sy;
                     const int cz = rem - cy * sy;
                     const int gx = pmod(w0[0] + cx, a.ng), gy = pmod(w0[1] + cy, a.ng), gz = pmod(w0[2] + cz, a.ng);
-                    win[cidx] = __ldg(a.t3f + ((gx + a.halo) * a.ext + gy + a.halo) * a.ext + gz + a.halo);
+                    long long cell = ((long long)(gx + a.halo) * a.ext + gy + a.halo) * a.ext + gz + a.halo;
+                    STEPS_CHECK_IDX(cell, (long long)a.ext * a.ext * a.ext, CK_T3_CELL);
+                    win[cidx] = __ldg(a.t3f + cell);
                 }
             }
             __syncthreads();
@@ -292,6 +295,11 @@ __global__ void __launch_bounds__(BLOCK) k_pair_t3(MixedArgs a)
                             bx = min(max((int)fxl - OFF, 0), wn[0] - NT);
                             by = min(max((int)fyl - OFF, 0), wn[1] - NT);
                             bz = min(max((int)fzl - OFF, 0), wn[2] - NT);
+#ifdef STEPS_CHECK
+                            const long long wfirst = bx * sx + by * sy + bz;
+                            if (!check_span(wfirst, wfirst + (NT - 1) * (sx + sy + 1), ncell, CK_T3_CELL))
+                                bx = by = bz = 0;
+#endif
                             const float4 *base = win + (bx * sx + by * sy + bz);
                             stencil<ORDER>(wx, wy, wz, [&](int aa, int bb, int cc) { return base[aa * sx + bb * sy + cc]; },
                                            Dx, Dy, Dz);
@@ -306,6 +314,12 @@ __global__ void __launch_bounds__(BLOCK) k_pair_t3(MixedArgs a)
                             bx = min(max((int)fxl - OFF, 0), E - NT);
                             by = min(max((int)fyl - OFF, 0), E - NT);
                             bz = min(max((int)fzl - OFF, 0), E - NT);
+#ifdef STEPS_CHECK
+                            const long long hfirst = ((long long)bx * E + by) * E + bz;
+                            if (!check_span(hfirst, hfirst + (long long)(NT - 1) * ((long long)E * E + E + 1),
+                                            (long long)E * E * E, CK_T3_CELL))
+                                bx = by = bz = 0;
+#endif
                             if (ORDER == 4) {
                                 // z-row records: the 4 z taps of one (x, y) row, per
                                 // component, in 3 float4 (48 B), 16 rows per pair
@@ -358,6 +372,9 @@ __global__ void __launch_bounds__(BLOCK) k_pair_t3(MixedArgs a)
                                 gx[t] = wrap_index(bx + t, a.ng) + a.halo;
                                 gy[t] = wrap_index(by + t, a.ng) + a.halo;
                                 gz[t] = wrap_index(bz + t, a.ng) + a.halo;
+                                STEPS_CHECK_IDX(gx[t], a.ext, CK_T3_CELL);
+                                STEPS_CHECK_IDX(gy[t], a.ext, CK_T3_CELL);
+                                STEPS_CHECK_IDX(gz[t], a.ext, CK_T3_CELL);
                             }
                             stencil<ORDER>(wx, wy, wz,
                                            [&](int aa, int bb, int cc) {
@@ -422,7 +439,9 @@ __device__ __forceinline__ void s1r2_interp_f32(const float2 *__restrict__ T, co
     if (ORDER == 0) {
         int ir = (int)floorf(ur + 0.5f);
         ir = ir < 0 ? 0 : (ir > nrho - 1 ? nrho - 1 : ir);
-        const int izc = wrap_near(floorf(uz + 0.5f), nz);
+        int izc = wrap_near(floorf(uz + 0.5f), nz);
+        STEPS_CHECK_IDX(ir, nrho, CK_S1_CELL);
+        STEPS_CHECK_IDX(izc, nz, CK_S1_CELL);
         const float2 v = __ldg(T + (size_t)ir * nz + izc);
         Dr = v.x;
         Dz = v.y;
@@ -433,9 +452,14 @@ __device__ __forceinline__ void s1r2_interp_f32(const float2 *__restrict__ T, co
         if (ir0 > nrho - 2) { ir0 = nrho - 2 > 0 ? nrho - 2 : 0; fr = 1.0f; }
         const float iz0r = floorf(uz);
         const float fz = uz - iz0r;
-        const int iz0 = wrap_near(iz0r, nz), iz1 = iz0 + 1 < nz ? iz0 + 1 : 0;
+        const int iz0 = wrap_near(iz0r, nz);
+        int iz1 = iz0 + 1 < nz ? iz0 + 1 : 0;
+        int ra = ir0, rb = ir0 + 1;
+        STEPS_CHECK_IDX(ra, nrho, CK_S1_CELL);
+        STEPS_CHECK_IDX(rb, nrho, CK_S1_CELL);
+        STEPS_CHECK_IDX(iz1, nz, CK_S1_CELL);
         // record (ir, iz0 + 1) starts with cells iz0, iz0 + 1
-        const float4 r0 = __ldg(R + 2 * ((size_t)ir0 * nz + iz1)), r1 = __ldg(R + 2 * ((size_t)(ir0 + 1) * nz + iz1));
+        const float4 r0 = __ldg(R + 2 * ((size_t)ra * nz + iz1)), r1 = __ldg(R + 2 * ((size_t)rb * nz + iz1));
         const float w00 = (1.0f - fr) * (1.0f - fz), w10 = fr * (1.0f - fz), w01 = (1.0f - fr) * fz, w11 = fr * fz;
         Dr = w00 * r0.x + w10 * r1.x + w01 * r0.z + w11 * r1.z;
         Dz = w00 * r0.y + w10 * r1.y + w01 * r0.w + w11 * r1.w;
@@ -449,7 +473,10 @@ __device__ __forceinline__ void s1r2_interp_f32(const float2 *__restrict__ T, co
         if (ir[1] < 0) ir[1] = 0;
         if (ir[1] > nrho - 1) ir[1] = nrho - 1;
         if (ir[2] > nrho - 1) ir[2] = nrho - 1;
-        const int iz1 = wrap_near((float)jz, nz);
+        int iz1 = wrap_near((float)jz, nz);
+        STEPS_CHECK_IDX(iz1, nz, CK_S1_CELL);
+#pragma unroll
+        for (int r = 0; r < 3; r++) STEPS_CHECK_IDX(ir[r], nrho, CK_S1_CELL);
 #pragma unroll
         for (int r = 0; r < 3; r++) {  // record (ir, iz1): cells iz1 - 1, iz1, iz1 + 1
             const float4 *rec = R + 2 * ((size_t)ir[r] * nz + iz1);
@@ -517,7 +544,8 @@ __global__ void __launch_bounds__(BLOCK) k_pair_s1tab(MixedArgs a)
         __syncthreads();
         const int item = s_item;
         if (item >= a.nitems) return;
-        const int I = (item / a.S) * a.istride;
+        int I = (item / a.S) * a.istride;
+        STEPS_CHECK_IDX(I, a.nit, CK_I_TILE);
         const int chunk = item % a.S;
         const int J0 = chunk * a.tpc;
         const int J1 = min(a.njt, J0 + a.tpc);
@@ -640,6 +668,8 @@ __global__ void __launch_bounds__(BLOCK) k_pair_s1tab(MixedArgs a)
                                 izc = ngp_z_index(dz64, uzc, a);
                             }
                         }
+                        STEPS_CHECK_IDX(ir, a.nrho, CK_S1_CELL);
+                        STEPS_CHECK_IDX(izc, a.nz, CK_S1_CELL);
                         const float2 v = __ldg(tab + (size_t)ir * a.nz + izc);
                         Dr = v.x;
                         Dz = v.y;
@@ -715,6 +745,259 @@ __global__ void k_table_f32(const double *__restrict__ t, int ng, int halo, floa
     out[c] = make_float4((float)t[3 * s], (float)t[3 * s + 1], (float)t[3 * s + 2], 0.0f);
 }
 
+// Ewald correction D(d) of one pair from the FP32 table (not the window):
+// stencil records of the haloed copy when the tile pair's stencils stay in
+// the halo, else taps of the haloed copy at indices wrapped once per axis.
+template <int ORDER>
+__device__ __forceinline__ void t3_correction(const MixedArgs &a, bool halo, float dx, float dy, float dz, float &Dx,
+                                              float &Dy, float &Dz)
+{
+    constexpr int NT = ORDER;
+    constexpr int OFF = ORDER == 4 ? 1 : 0;
+    float wx[4], wy[4], wz[4];
+    Dx = Dy = Dz = 0.0f;
+    if (halo) {
+        const float uh = a.u0 + (float)a.halo;
+        const float ux = fmaf(dx, a.ih, uh), uy = fmaf(dy, a.ih, uh), uz = fmaf(dz, a.ih, uh);
+        const float fxl = floorf(ux), fyl = floorf(uy), fzl = floorf(uz);
+        weights<ORDER>(ux - fxl, wx);
+        weights<ORDER>(uy - fyl, wy);
+        weights<ORDER>(uz - fzl, wz);
+        const int E = a.ext;
+        int bx = min(max((int)fxl - OFF, 0), E - NT);
+        int by = min(max((int)fyl - OFF, 0), E - NT);
+        int bz = min(max((int)fzl - OFF, 0), E - NT);
+#ifdef STEPS_CHECK
+        const long long hfirst = ((long long)bx * E + by) * E + bz;
+        if (!check_span(hfirst, hfirst + (long long)(NT - 1) * ((long long)E * E + E + 1), (long long)E * E * E,
+                        CK_T3_CELL))
+            bx = by = bz = 0;
+#endif
+        const float4 *rbase = a.t3r + 3 * ((bx * E + by) * E + bz);
+        if (ORDER == 4) {  // z-row records
+#pragma unroll
+            for (int aa = 0; aa < 4; aa++) {
+                float rx = 0.0f, ry = 0.0f, rz = 0.0f;
+#pragma unroll
+                for (int bb = 0; bb < 4; bb++) {
+                    const float4 *r = rbase + 3 * (aa * E + bb) * E;
+                    const float4 vx = __ldg(r), vy = __ldg(r + 1), vz = __ldg(r + 2);
+                    rx = fmaf(wy[bb], dot4(wz, vx), rx);
+                    ry = fmaf(wy[bb], dot4(wz, vy), ry);
+                    rz = fmaf(wy[bb], dot4(wz, vz), rz);
+                }
+                Dx = fmaf(wx[aa], rx, Dx);
+                Dy = fmaf(wx[aa], ry, Dy);
+                Dz = fmaf(wx[aa], rz, Dz);
+            }
+        } else {  // (y, z) quad records
+            const float q00 = wy[0] * wz[0], q01 = wy[0] * wz[1], q10 = wy[1] * wz[0], q11 = wy[1] * wz[1];
+#pragma unroll
+            for (int aa = 0; aa < 2; aa++) {
+                const float4 *r = rbase + 3 * aa * E * E;
+                const float4 vx = __ldg(r), vy = __ldg(r + 1), vz = __ldg(r + 2);
+                Dx = fmaf(wx[aa], fmaf(q11, vx.w, fmaf(q10, vx.z, fmaf(q01, vx.y, q00 * vx.x))), Dx);
+                Dy = fmaf(wx[aa], fmaf(q11, vy.w, fmaf(q10, vy.z, fmaf(q01, vy.y, q00 * vy.x))), Dy);
+                Dz = fmaf(wx[aa], fmaf(q11, vz.w, fmaf(q10, vz.z, fmaf(q01, vz.y, q00 * vz.x))), Dz);
+            }
+        }
+    } else {
+        const float ux = fmaf(dx, a.ih, a.u0), uy = fmaf(dy, a.ih, a.u0), uz = fmaf(dz, a.ih, a.u0);
+        const float fxl = floorf(ux), fyl = floorf(uy), fzl = floorf(uz);
+        weights<ORDER>(ux - fxl, wx);
+        weights<ORDER>(uy - fyl, wy);
+        weights<ORDER>(uz - fzl, wz);
+        const int bx = (int)fxl - OFF, by = (int)fyl - OFF, bz = (int)fzl - OFF;
+        int gx[NT], gy[NT], gz[NT];
+#pragma unroll
+        for (int t = 0; t < NT; t++) {
+            gx[t] = wrap_index(bx + t, a.ng) + a.halo;
+            gy[t] = wrap_index(by + t, a.ng) + a.halo;
+            gz[t] = wrap_index(bz + t, a.ng) + a.halo;
+            STEPS_CHECK_IDX(gx[t], a.ext, CK_T3_CELL);
+            STEPS_CHECK_IDX(gy[t], a.ext, CK_T3_CELL);
+            STEPS_CHECK_IDX(gz[t], a.ext, CK_T3_CELL);
+        }
+        stencil<ORDER>(wx, wy, wz,
+                       [&](int aa, int bb, int cc) { return __ldg(a.t3f + (gx[aa] * a.ext + gy[bb]) * a.ext + gz[cc]); },
+                       Dx, Dy, Dz);
+    }
+}
+
+// Quad lane mapping (T^3 variant 1, one i per thread). The 32 lanes of a warp
+// form 8 quads; quad g holds the warp's i particles 4g..4g+3 (one per lane).
+// In each step every lane of quad g takes the same i, 4g + s for s = 0..3 in
+// turn, against its own j, jb + (lane & 3). One table-record load then serves
+// 8 distinct i against 4 neighbouring j instead of 32 i against one j, and
+// the lanes' stencils share more L1 lines. Each lane keeps 4 FP32 partial
+// forces (one per i of its quad) over a j tile; a 4-lane transpose-reduce
+// (3 shuffles per component) leaves every lane the sum for its own i, which
+// goes into the FP64 accumulator as in the one-i-per-lane kernel.
+template <int BLOCK, int ORDER>
+__global__ void __launch_bounds__(BLOCK) k_pair_t3q(MixedArgs a)
+{
+    constexpr int T = BLOCK;
+    constexpr int NT = ORDER;
+    constexpr int OFF = ORDER == 4 ? 1 : 0;
+    constexpr unsigned FULL = 0xffffffffu;
+    __shared__ __align__(16) float4 sp[2][T];
+    __shared__ __align__(16) float se[2][T];
+    __shared__ __align__(16) uint32_t sid[2][T];
+    __shared__ __align__(16) float4 sres[2][T];
+    __shared__ int s_item;
+    const int tid = threadIdx.x, lane = tid & 31, r = lane & 3, qb = lane & ~3;
+    const float L = a.L, halfL = a.halfL;
+
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) s_item = (int)atomicAdd(a.counter, 1u);
+        __syncthreads();
+        const int item = s_item;
+        if (item >= a.nitems) return;
+        int I = (item / a.S) * a.istride;
+        STEPS_CHECK_IDX(I, a.nit, CK_I_TILE);
+        const int chunk = item % a.S;
+        const int J0 = chunk * a.tpc;
+        const int J1 = min(a.njt, J0 + a.tpc);
+
+        const float4 mI0 = __ldg(a.imeta + 2 * I);
+        const float4 mI1 = __ldg(a.imeta + 2 * I + 1);
+        const size_t qi = (size_t)I * T + tid;
+        const float4 pi = __ldg(a.ipack + qi);
+        const float4 li = __ldg(a.ilo + qi);
+        const float eown = __ldg(a.ieps + qi);
+        const uint32_t idown = __ldg(a.iidx + qi);
+        // this quad's softening and ids (constant over the item)
+        float E4[4];
+        uint32_t Id4[4];
+#pragma unroll
+        for (int s = 0; s < 4; s++) {
+            E4[s] = __shfl_sync(FULL, eown, qb | s);
+            Id4[s] = __shfl_sync(FULL, idown, qb | s);
+        }
+        double ax = 0.0, ay = 0.0, az = 0.0;
+
+        if (J0 < J1) stage_tile<BLOCK, 1>(a, J0, sp[0], se[0], sid[0], sres[0]);
+        for (int J = J0; J < J1; ++J) {
+            const int buf = (J - J0) & 1;
+            const float4 mJ0 = __ldg(a.jmeta + 2 * J);
+            const float4 mJ1 = __ldg(a.jmeta + 2 * J + 1);
+            float eO[3];
+            float dO[3] = {two_diff(mJ0.x, mI0.x, eO[0]), two_diff(mJ0.y, mI0.y, eO[1]),
+                           two_diff(mJ0.z, mI0.z, eO[2])};
+            const float hs[3] = {mI1.x + mJ1.x, mI1.y + mJ1.y, mI1.z + mJ1.z};
+            bool wrap[3];
+            float g2 = 0.0f;
+            bool halo = ORDER != 0;
+#pragma unroll
+            for (int ax3 = 0; ax3 < 3; ax3++) {
+                shift_frame(dO[ax3], eO[ax3], L, a.L_lo);  // nearest image of J's centre
+                wrap[ax3] = fabsf(dO[ax3]) + hs[ax3] > halfL - a.wrap_tol;
+                const float g = fmaxf(fabsf(dO[ax3]) - hs[ax3], 0.0f);
+                g2 += g * g;
+                const int w0 = (int)floorf((dO[ax3] - hs[ax3]) * a.ih + a.u0 - 1e-3f) - OFF;
+                const int w1 = (int)floorf((dO[ax3] + hs[ax3]) * a.ih + a.u0 + 1e-3f) - OFF + NT;
+                halo = halo && w0 >= -a.halo && w1 <= a.ng + a.halo;
+            }
+            const float bmax = mI0.w + mJ0.w;
+            const bool full = g2 <= bmax * bmax * 1.0001f + 1e-30f || wrap[0] || wrap[1] || wrap[2] ||
+                              coarse_for_gap(dO[0], dO[1], dO[2], mI1, mJ1, g2, a.guard2);
+            if (J + 1 < J1) {
+                stage_tile<BLOCK, 1>(a, J + 1, sp[buf ^ 1], se[buf ^ 1], sid[buf ^ 1], sres[buf ^ 1]);
+                cp_wait<1>();
+            } else {
+                cp_wait<0>();
+            }
+            __syncthreads();
+
+            // own i in J's frame, then the quad's four
+            float phx, phy, phz, plx, ply, plz;
+            frame_split(pi.x, li.x, dO[0], eO[0], phx, plx);
+            frame_split(pi.y, li.y, dO[1], eO[1], phy, ply);
+            frame_split(pi.z, li.z, dO[2], eO[2], phz, plz);
+            float Hx[4], Hy[4], Hz[4], Lx[4], Ly[4], Lz[4];
+#pragma unroll
+            for (int s = 0; s < 4; s++) {
+                Hx[s] = __shfl_sync(FULL, phx, qb | s);
+                Hy[s] = __shfl_sync(FULL, phy, qb | s);
+                Hz[s] = __shfl_sync(FULL, phz, qb | s);
+                Lx[s] = __shfl_sync(FULL, plx, qb | s);
+                Ly[s] = __shfl_sync(FULL, ply, qb | s);
+                Lz[s] = __shfl_sync(FULL, plz, qb | s);
+            }
+            float fx[4] = {0.0f, 0.0f, 0.0f, 0.0f}, fy[4] = {0.0f, 0.0f, 0.0f, 0.0f},
+                  fz[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+            const float4 *spb = sp[buf];
+            const float *seb = se[buf];
+            const uint32_t *sidb = sid[buf];
+            const float4 *sresb = sres[buf];
+
+#pragma unroll 1
+            for (int jb = 0; jb < T; jb += 4) {
+                const int jj = jb + r;
+                const float4 q = spb[jj];
+                const float ej = seb[jj];
+                const uint32_t jid = sidb[jj];
+                const float4 ql = full ? sresb[jj] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+                for (int s = 0; s < 4; s++) {
+                    const bool self = full && jid == Id4[s];
+                    float dx, dy, dz;
+                    if (full) {  // double-float separation
+                        dx = self ? 0.0f : (q.x - Hx[s]) + (ql.x - Lx[s]);
+                        dy = self ? 0.0f : (q.y - Hy[s]) + (ql.y - Ly[s]);
+                        dz = self ? 0.0f : (q.z - Hz[s]) + (ql.z - Lz[s]);
+                    } else {
+                        dx = q.x - (Hx[s] + Lx[s]);
+                        dy = q.y - (Hy[s] + Ly[s]);
+                        dz = q.z - (Hz[s] + Lz[s]);
+                    }
+                    float nx = dx, ny = dy, nz = dz;
+                    if (full && !self) {  // wrapped axes are full-path tile pairs
+                        if (wrap[0]) nx = nearest_image(dx, q.x, Hx[s], ql.x, Lx[s], L, halfL, a.halfL_lo, a.wrap_tol);
+                        if (wrap[1]) ny = nearest_image(dy, q.y, Hy[s], ql.y, Ly[s], L, halfL, a.halfL_lo, a.wrap_tol);
+                        if (wrap[2]) nz = nearest_image(dz, q.z, Hz[s], ql.z, Lz[s], L, halfL, a.halfL_lo, a.wrap_tol);
+                    }
+                    const float r2 = fmaf(nx, nx, fmaf(ny, ny, nz * nz));
+                    const float ri = rsqrt_mufu(r2);
+                    float w = ri * ri * ri;
+                    if (full) {
+                        const float b = E4[s] + ej;
+                        if (r2 < b * b) w = spline_inner_f32(r2, b);
+                    }
+                    float Dx = 0.0f, Dy = 0.0f, Dz = 0.0f;
+                    if (ORDER != 0) t3_correction<ORDER>(a, halo, dx, dy, dz, Dx, Dy, Dz);
+                    fx[s] = fmaf(q.w, fmaf(w, nx, -Dx), fx[s]);
+                    fy[s] = fmaf(q.w, fmaf(w, ny, -Dy), fy[s]);
+                    fz[s] = fmaf(q.w, fmaf(w, nz, -Dz), fz[s]);
+                }
+            }
+            // 4-lane transpose-reduce: lane r = 2b + c ends with the sum of
+            // element r over its quad
+            const bool b = (r & 2) != 0, c = (r & 1) != 0;
+            float h0, h1, tx, ty, tz;
+            h0 = (b ? fx[2] : fx[0]) + __shfl_xor_sync(FULL, b ? fx[0] : fx[2], 2);
+            h1 = (b ? fx[3] : fx[1]) + __shfl_xor_sync(FULL, b ? fx[1] : fx[3], 2);
+            tx = (c ? h1 : h0) + __shfl_xor_sync(FULL, c ? h0 : h1, 1);
+            h0 = (b ? fy[2] : fy[0]) + __shfl_xor_sync(FULL, b ? fy[0] : fy[2], 2);
+            h1 = (b ? fy[3] : fy[1]) + __shfl_xor_sync(FULL, b ? fy[1] : fy[3], 2);
+            ty = (c ? h1 : h0) + __shfl_xor_sync(FULL, c ? h0 : h1, 1);
+            h0 = (b ? fz[2] : fz[0]) + __shfl_xor_sync(FULL, b ? fz[0] : fz[2], 2);
+            h1 = (b ? fz[3] : fz[1]) + __shfl_xor_sync(FULL, b ? fz[1] : fz[3], 2);
+            tz = (c ? h1 : h0) + __shfl_xor_sync(FULL, c ? h0 : h1, 1);
+            ax += (double)tx;
+            ay += (double)ty;
+            az += (double)tz;
+            __syncthreads();
+        }
+
+        double *o = a.part + (size_t)chunk * a.part_stride;
+        o[3 * qi] = ax;
+        o[3 * qi + 1] = ay;
+        o[3 * qi + 2] = az;
+    }
+}
+
 template <int ORDER>
 KernelFn pick_t3(int threads, int ipt)
 {
@@ -727,10 +1010,21 @@ KernelFn pick_t3(int threads, int ipt)
 
 }  // namespace
 
-KernelFn t3_kernel(const KParams &kp, int threads, int ipt, size_t *dyn_smem)
+KernelFn t3_quad_kernel(const KParams &kp, int threads, int ipt)
+{
+    if (kp.is_periodic < 2 || kp.order != 2 || ipt != 1) return nullptr;  // trilinear, one i per thread
+    if (threads == 64) return k_pair_t3q<64, 2>;
+    if (threads == 128) return k_pair_t3q<128, 2>;
+    if (threads == 256) return k_pair_t3q<256, 2>;
+    return nullptr;
+}
+
+KernelFn t3_kernel(const KParams &kp, int threads, int ipt, size_t *dyn_smem, int variant)
 {
     *dyn_smem = 0;
     if (kp.is_periodic < 2) return pick_t3<0>(threads, ipt);
+    if (variant == 1)  // quad lanes where they exist (no shared-memory window)
+        if (KernelFn q = t3_quad_kernel(kp, threads, ipt)) return q;
     *dyn_smem = (size_t)ctx().shape.t3_cells * sizeof(float4);
     return kp.order == 4 ? pick_t3<4>(threads, ipt) : pick_t3<2>(threads, ipt);
 }

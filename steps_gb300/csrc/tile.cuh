@@ -22,12 +22,14 @@ __device__ __forceinline__ double warp_max(double v)
 // padded to T) with a block of NT threads: FP32-exact centre, half extents and
 // largest softening (meta), FP32 offsets (pack, soa), their FP32 residuals
 // (lo), softening (epsf), original indices (idx) and the sub-tile boxes (sub).
+// perm holds original indices below nx (checked in bounds-checked builds).
 // COH: positions are read through L2 (ld.global.cg), for a kernel in which
 // other blocks have just written them (L1 is not coherent across SMs).
 template <int NT, bool COH>
 __device__ __forceinline__ void build_tile(int tile, int sbase, int cnt, const double *__restrict__ x,
                                            const double *__restrict__ m, const double *__restrict__ eps,
-                                           const uint32_t *__restrict__ perm, int T, float4 *__restrict__ pack,
+                                           const uint32_t *__restrict__ perm, long long nx, int T,
+                                           float4 *__restrict__ pack,
                                            float *__restrict__ epsf, float4 *__restrict__ meta,
                                            uint32_t *__restrict__ idx, uint32_t pad_id, float4 *__restrict__ lo,
                                            float *__restrict__ soa, float4 *__restrict__ sub)
@@ -40,6 +42,7 @@ __device__ __forceinline__ void build_tile(int tile, int sbase, int cnt, const d
     for (int e = t; e < T; e += NT) {
         if (e < cnt) {
             uint32_t o = perm[sbase + e];
+            STEPS_CHECK_IDX(o, nx, CK_PERM);
             for (int k = 0; k < 3; k++) {
                 double v = ldx(3 * (size_t)o + k);
                 mn[k] = fmin(mn[k], v);
@@ -80,6 +83,7 @@ __device__ __forceinline__ void build_tile(int tile, int sbase, int cnt, const d
         const int q = tile * T + e;
         if (e < cnt) {
             uint32_t o = perm[sbase + e];
+            STEPS_CHECK_IDX(o, nx, CK_PERM);
             const double ox = ldx(3 * (size_t)o) - cx, oy = ldx(3 * (size_t)o + 1) - cy, oz = ldx(3 * (size_t)o + 2) - cz;
             const float hx = __double2float_rn(ox), hy = __double2float_rn(oy), hz = __double2float_rn(oz);
             pack[q] = make_float4(hx, hy, hz, __double2float_rn(m[o]));

@@ -81,3 +81,18 @@ def test_header_is_plain_c_and_links(tmp_path, lib):
                         os.path.join(ROOT, "include"), str(src), "-o", str(exe), "-L", lib_dir, "-lsteps_gb300",
                         "-Wl,--no-undefined"], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-2000:]
+
+
+def test_bounds_checked_library_exports_the_same_symbols(lib):
+    """The -DSTEPS_CHECK build is the same C-ABI; only it reports checks
+    compiled in (nothing that touches the GPU is called)."""
+    import steps_gb300 as S
+
+    if not os.path.exists(S.CHECK_LIB_PATH):
+        from steps_gb300 import build
+        build.build()
+    chk = ctypes.CDLL(S.CHECK_LIB_PATH)
+    missing = [n for n in declared_symbols() if not hasattr(chk, n)]
+    assert not missing, f"not exported by the checked build: {missing}"
+    assert chk.steps_gpu_checks_compiled() == 1
+    assert lib.steps_gpu_checks_compiled() == 0

@@ -125,3 +125,27 @@ def test_cfg0_force_and_four_kdk_steps(engine, port):
             assert np.abs(dg - do).max() <= 1e-3 * np.abs(do).max()
             assert err_stats(F, Fo)["p99"] < 1e-5
             assert abs(e - eo) <= 1e-4 * abs(eo)
+
+
+def test_kdk_mixed_reuses_order_across_resorts(engine):
+    """20 mixed R^3 steps, with velocities that carry particles across tiles:
+    the steps between re-sorts rebuild the tiles in the previous order. The
+    forces the run ends with match the FP64 kernel at the final positions,
+    and the trajectory tracks an FP64 run of the same steps."""
+    from steps_gb300 import workloads as W
+
+    ps = W.r3_compactified(20000, 480.0, seed=5, displace=True)
+    v0 = np.random.default_rng(5).normal(0.0, 2000.0, ps.x.shape)
+    engine.set_particles(ps.m, ps.eps)
+    runs = {}
+    for precision in (S.FP64, S.MIXED):
+        engine.upload_positions(ps.x)
+        engine.upload_velocities(v0)
+        engine.kdk(S.params(S.R3), precision, 20, 1e-3)
+        runs[precision] = engine.state()
+    x, v, F = runs[S.MIXED]
+    x64, v64, _ = runs[S.FP64]
+    assert np.abs(x - ps.x).max() > 10.0  # particles moved by many softening lengths
+    assert err_stats(F, engine.forces(x, S.params(S.R3), S.FP64))["p99"] < 1e-5
+    assert np.abs(x - x64).max() < 1e-6 * (1 + np.abs(x64).max())
+    assert err_stats(v - v0, v64 - v0)["p99"] < 1e-4

@@ -246,7 +246,15 @@ def test_t3_mixed_shapes_and_workload_table(engine, port, order):
                 engine.set_tuning(threads, ipt, 0)
                 st = err_stats(engine.forces(ps.x, p, S.MIXED), F64)
                 assert st["p99"] < MIXED_P99, (cells, threads, ipt, st)
+        # quad lanes (trilinear; tricubic falls back to one i per lane)
+        engine.set_t3_window(0)
+        engine.set_variant(1)
+        for threads in (64, 128, 256):
+            engine.set_tuning(threads, 1, 0)
+            st = err_stats(engine.forces(ps.x, p, S.MIXED), F64)
+            assert st["p99"] < MIXED_P99, ("quad", threads, st)
     finally:
+        engine.set_variant(0)
         engine.set_tuning(128, 2, 0)
         engine.set_t3_window(0)
 
@@ -282,9 +290,16 @@ def test_t3_nearest_image_at_half_box(engine, isp):
     engine.set_table_t3(g["table"], ng)
     p = S.params(S.T3, is_periodic=isp, L=L, rsim=L / 2, ewald_order=2)
     F64 = engine.forces(x, p, S.FP64)
-    e = rel_err(engine.forces(x, p, S.MIXED), F64)
-    assert np.percentile(e[:2048], 99) < MIXED_P99 and np.percentile(e, 99) < MIXED_P99, (
-        np.percentile(e[:2048], [50, 99, 100]))
+    try:
+        for variant in (0, 1):  # one i per lane; quad lanes
+            engine.set_variant(variant)
+            engine.set_tuning(128, 1 if variant else 2, 0)
+            e = rel_err(engine.forces(x, p, S.MIXED), F64)
+            assert np.percentile(e[:2048], 99) < MIXED_P99 and np.percentile(e, 99) < MIXED_P99, (
+                variant, np.percentile(e[:2048], [50, 99, 100]))
+    finally:
+        engine.set_variant(0)
+        engine.set_tuning(128, 2, 0)
 
 
 @pytest.mark.parametrize("mode", ["nearest", "table"])
