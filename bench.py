@@ -261,6 +261,8 @@ def cpu_baseline(ps, p, sample: int, threads: int, table=None, seconds: float = 
         probe = min(max(2 * probe, int(probe * target / max(dt, 1e-9))), ps.n - lo)
     if sample <= 0:
         sample = int(probe * seconds / max(dt, 1e-9))
+    # whole rounds of the thread team, at least 4 i per thread (OpenMP static schedule)
+    sample = max(4 * threads, -(-sample // threads) * threads)
     sample = max(8, min(sample, ps.n - lo))
     hi = lo + sample - 1
     t0 = time.perf_counter()

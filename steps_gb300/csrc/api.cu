@@ -572,9 +572,10 @@ int steps_gpu_autotune(const steps_params *p, int id_min, int id_max, int *out)
                          : kp.topology == STEPS_T3 && kp.is_periodic >= 2 ? T3_VARIANTS
                                                                           : 1;
         // Stage 1: each candidate is scored by its time per pair on a strided
-        // sample of the real i tiles, 24 waves of items (one untimed launch,
-        // one timed; the whole range if it is smaller). Fewer waves misrank
-        // the candidates: the launch ramp and the last wave weigh in.
+        // sample of the real i tiles, 24 waves of items (one untimed one-wave
+        // launch, then one timed; the whole range if it is smaller). Fewer
+        // waves misrank the candidates: the launch ramp and the last wave
+        // weigh in.
         // Stage 2: the three best are timed on 96 waves (or the whole range).
         struct SampleMode {
             Ctx &c;
@@ -586,17 +587,20 @@ int steps_gpu_autotune(const steps_params *p, int id_min, int id_max, int *out)
                 c.F_valid = false;
             }
         } mode(c);
-        // time per pair of one timed launch at a sample size (after `warm` untimed ones)
-        auto score = [&](const Shape &sh, int waves, int warm) {
+        // time per pair of one timed launch at a sample size; warm: after an
+        // untimed one-wave launch (module load, caches)
+        auto score = [&](const Shape &sh, int waves, bool warm) {
             c.shape = sh;
+            if (warm) {
+                c.tune_sample = 1;
+                compute_forces(p, STEPS_MIXED, id_min, id_max, true);
+            }
             c.tune_sample = waves;
             float ms = 0.0f;
-            for (int r = 0; r <= warm; r++) {
-                // the phase events bracket the pair kernel only
-                compute_forces(p, STEPS_MIXED, id_min, id_max, true);
-                STEPS_CUDA(cudaEventSynchronize(c.phase[2]));
-                STEPS_CUDA(cudaEventElapsedTime(&ms, c.phase[1], c.phase[2]));
-            }
+            // the phase events bracket the pair kernel only
+            compute_forces(p, STEPS_MIXED, id_min, id_max, true);
+            STEPS_CUDA(cudaEventSynchronize(c.phase[2]));
+            STEPS_CUDA(cudaEventElapsedTime(&ms, c.phase[1], c.phase[2]));
             return (double)ms / c.last_pairs;
         };
         c.tune_sample = 1;
@@ -614,13 +618,21 @@ int steps_gpu_autotune(const steps_params *p, int id_min, int id_max, int *out)
                 sh.ipt = s[1];
                 sh.jsplit = 0;
                 sh.variant = v;
-                scored.emplace_back(score(sh, 24, 1), sh);
+                scored.emplace_back(score(sh, 24, true), sh);
+                // A range of few waves is balanced by its shortest items:
+                // there the j split is timed too (2x and 4x the rule's chunks).
+                const int rule_S = c.last_S;
+                if (c.last_waves < 32.0)
+                    for (int f = 2; f <= 4; f *= 2) {
+                        sh.jsplit = rule_S * f;
+                        scored.emplace_back(score(sh, 24, true), sh);
+                    }
             }
         std::stable_sort(scored.begin(), scored.end(), [](const std::pair<double, Shape> &a,
                                                           const std::pair<double, Shape> &b) { return a.first < b.first; });
         double best = 1e300;
         for (size_t k = 0; k < scored.size() && k < 3; k++) {
-            const double sc = score(scored[k].second, 96, 0);
+            const double sc = score(scored[k].second, 96, false);
             if (sc < best) { best = sc; bestS = scored[k].second; }
         }
         c.shape = bestS;

@@ -56,6 +56,8 @@ struct Ctx {
                           // i tiles (0: off), no reduction
     bool tune_sampled = false;  // the last timing run was cut to a sample (else it covered the whole range)
     double last_pairs = 0.0;
+    int last_S = 0;             // j chunks per i tile of the last mixed launch
+    double last_waves = 0.0;    // its full-range items over the resident blocks
 
     Batch *batch = nullptr;
 };

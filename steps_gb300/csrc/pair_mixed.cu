@@ -490,19 +490,20 @@ void forces_mixed(const KParams &kp, const Tables &tb, const double *x, const do
     const int resident = c.nsm * occ;
     const int nit = ti.ntiles, njt = c.tj.ntiles;
     int S = c.shape.jsplit;
+    // The FP64 chunk partials (S x N_i x 24 B) stay within 4 GiB.
+    const long long smax = std::max(1LL, (4LL << 30) / ((long long)nit * T * 24));
     if (S <= 0) {
         // Items of at most 64 and at least 4 j tiles, aiming at 16 or more
         // waves of items over the persistent grid: long items balance badly
         // (near-field tile pairs make their lengths uneven), very short ones
-        // pay the per-item set-up. The FP64 chunk partials (S x N_i x 24 B)
-        // stay within 4 GiB.
-        const long long smax = std::max(1LL, (4LL << 30) / ((long long)nit * T * 24));
+        // pay the per-item set-up.
         const long long pairs = (long long)nit * njt;
         const long long tpc = std::min(64LL, std::max(4LL, pairs / (16LL * resident)));
         S = (int)std::min<long long>(smax, (njt + tpc - 1) / tpc);
         if (S < 1) S = 1;
     }
     if (S > njt) S = njt;
+    if (S > smax) S = (int)smax;
     const int tpc = div_up(njt, S);
     S = div_up(njt, tpc);
 
@@ -590,6 +591,8 @@ void forces_mixed(const KParams &kp, const Tables &tb, const double *x, const do
     STEPS_CUDA(cudaEventRecord(c.phase[3], st));
     c.phase_valid = true;
     c.last_pairs = c.tune_sampled ? (double)a.nitems * T * ((double)tpc * T) : (double)ni * (double)n;
+    c.last_S = S;
+    c.last_waves = (double)nit * S / resident;
 }
 
 }  // namespace steps
