@@ -488,9 +488,21 @@ def measure(eng, S, ps, p, flops, table, steps, warmup, fp64_sample, f32_peak, f
 
 
 def shape_desc(shape, args):
+    """The kernel shape; the variant names the R^3 pair loop, or for T^3 with
+    a table the lane mapping (the other workloads have one pair loop)."""
+    w = getattr(args, "workload", "cfg1")
+    table_t3 = w == "cfg3"
+
+    def loop(v):
+        if w in ("cfg0", "cfg1", "cfg4"):
+            return LOOPS[v]
+        if table_t3:
+            return "quad lanes" if v == 1 else "one i per lane"
+        return "fp32"
+
     if shape:
-        return {"threads": shape[0], "ipt": shape[1], "pair_loop": LOOPS[shape[2]]}
-    return (args.shape or "128x2") + " " + LOOPS[max(args.variant, 0)]
+        return {"threads": shape[0], "ipt": shape[1], "pair_loop": loop(shape[2])}
+    return (args.shape or "128x2") + " " + loop(max(args.variant, 0))
 
 
 def traffic_of(workload_name, n, shape):
@@ -633,7 +645,7 @@ def kdk_measure(eng, S, W, ps, steps, warmup, f32_peak, nkdk=4, dt=1e-3):
     return {"workload": f"R3 compactified N={n} R_max=480 Mpc: one force evaluation + {nkdk} KDK steps at dt={dt} "
                         f"from rest (the workload as specified), mixed and FP64",
             "value": value, "unit": UNIT, "ms_per_step": res["mixed"]["ms_per_step"], "steps": steps,
-            "pairs_per_step": pairs, "kernel_shape": shape_desc(shape, argparse.Namespace(shape="", variant=-1)),
+            "pairs_per_step": pairs, "kernel_shape": shape_desc(shape, argparse.Namespace(shape="", variant=-1, workload="cfg0")),
             "autotune_s": t_tune,
             "roofline": {"bound": "fp32", "frac_of_step": value * 20 / f32_peak, "peak": f32_peak / 1e12,
                          "flops_per_pair": 20,

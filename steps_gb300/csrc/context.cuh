@@ -40,8 +40,9 @@ struct Ctx {
     DevBuf t3r;                // stencil records of the haloed copy (z rows / yz quads)
     long long t3r_version = -1;
     int t3r_order = 0;
-    DevBuf s1rec;              // S1xR2 table z-triplet records (CIC, TSC)
+    DevBuf s1rec;              // S1xR2 table records: whole CIC stencils or TSC z triplets
     long long s1rec_version = -1;
+    int s1rec_order = -1;             // layout of s1rec: CIC (2) or TSC (4)
     DevBuf s1r2;
     int nrho = 0, nz = 0;
     long long s1r2_version = 0;

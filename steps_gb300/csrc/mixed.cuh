@@ -50,7 +50,7 @@ struct MixedArgs {
     const float4 *t3r;  // stencil records of the haloed copy (3 float4 per cell)
     // S1xR2 (rho, z) correction table (FP32 float2 copy) and its geometry
     const float2 *s1tab;
-    const float4 *s1rec;  // z-triplet records of s1tab (CIC, TSC)
+    const float4 *s1rec;  // records of s1tab: whole CIC stencils (32 bytes), TSC z triplets
     int nrho, nz;
     float irho, iz, rho_max;  // 1 / drho, nz / L_z
     double s1_drho, s1_dzc, s1_L;  // rho and z cell sizes and L in FP64 (exact NGP face decisions)

@@ -422,10 +422,12 @@ __device__ __forceinline__ int wrap_near(float f, int nz)
 // (rho, z) table interpolation in FP32 from the float2 copy of the S1xR2
 // table: NGP / CIC / TSC exactly as StePS/src/ewald_space.cc:803-1000
 // (rho clamped to [0, rho_max], z index periodic).
-// CIC and TSC read z-triplet records R: record (ir, iz) = cells (ir, iz-1),
-// (ir, iz), (ir, iz+1), z periodic, as (Dr, Dz) pairs in 2 float4 (the last
-// two floats unused). One rho row of a stencil is then 1 (CIC) or 2 (TSC)
-// loads instead of 2 or 3.
+// CIC reads whole-stencil records (k_table2_cic): 2 loads from one 32-byte
+// sector per pair. TSC reads z-triplet records (k_table2_zrec): record
+// (ir, iz) = cells (ir, iz-1), (ir, iz), (ir, iz+1), z periodic, as (Dr, Dz)
+// pairs in 2 float4, so one rho row of its stencil is 2 loads instead of 3.
+// (Whole TSC stencils in 128-byte records -- 5 loads from one line -- were
+// 20 % slower: the table grows 4x and falls out of L1.)
 template <int ORDER>
 __device__ __forceinline__ void s1r2_interp_f32(const float2 *__restrict__ T, const float4 *__restrict__ R, int nrho,
                                                 int nz, float irho, float rho_max, float iz, float halfL, float rho,
@@ -452,14 +454,13 @@ __device__ __forceinline__ void s1r2_interp_f32(const float2 *__restrict__ T, co
         if (ir0 > nrho - 2) { ir0 = nrho - 2 > 0 ? nrho - 2 : 0; fr = 1.0f; }
         const float iz0r = floorf(uz);
         const float fz = uz - iz0r;
-        const int iz0 = wrap_near(iz0r, nz);
-        int iz1 = iz0 + 1 < nz ? iz0 + 1 : 0;
-        int ra = ir0, rb = ir0 + 1;
-        STEPS_CHECK_IDX(ra, nrho, CK_S1_CELL);
-        STEPS_CHECK_IDX(rb, nrho, CK_S1_CELL);
-        STEPS_CHECK_IDX(iz1, nz, CK_S1_CELL);
-        // record (ir, iz0 + 1) starts with cells iz0, iz0 + 1
-        const float4 r0 = __ldg(R + 2 * ((size_t)ra * nz + iz1)), r1 = __ldg(R + 2 * ((size_t)rb * nz + iz1));
+        int iz0 = wrap_near(iz0r, nz);
+        int ra = ir0;
+        STEPS_CHECK_IDX(ra, nrho - 1, CK_S1_CELL);
+        STEPS_CHECK_IDX(iz0, nz, CK_S1_CELL);
+        // record (ir0, iz0): rows ir0, ir0 + 1 x cells iz0, iz0 + 1 (periodic)
+        const float4 *rec = R + 2 * ((size_t)ra * nz + iz0);
+        const float4 r0 = __ldg(rec), r1 = __ldg(rec + 1);
         const float w00 = (1.0f - fr) * (1.0f - fz), w10 = fr * (1.0f - fz), w01 = (1.0f - fr) * fz, w11 = fr * fz;
         Dr = w00 * r0.x + w10 * r1.x + w01 * r0.z + w11 * r1.z;
         Dz = w00 * r0.y + w10 * r1.y + w01 * r0.w + w11 * r1.w;
@@ -702,7 +703,23 @@ __global__ void __launch_bounds__(BLOCK) k_pair_s1tab(MixedArgs a)
     }
 }
 
-// z-triplet records of the (rho, z) table (see s1r2_interp_f32).
+// CIC stencil records of the (rho, z) table: record (ir, iz) holds rows ir,
+// ir + 1 (clamped to the table) x cells iz, iz + 1 (periodic) as (D_rho, D_z)
+// pairs in 2 float4.
+__global__ void k_table2_cic(const double *__restrict__ t, int nrho, int nz, float4 *__restrict__ out)
+{
+    const size_t ncell = (size_t)nrho * nz;
+    size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncell) return;
+    const int iz = (int)(c % nz), ir = (int)(c / nz);
+    const int ir1 = ir + 1 < nrho ? ir + 1 : nrho - 1, iz1 = iz + 1 < nz ? iz + 1 : 0;
+    const size_t a = (size_t)ir * nz + iz, b = (size_t)ir * nz + iz1, d = (size_t)ir1 * nz + iz,
+                 e = (size_t)ir1 * nz + iz1;
+    out[2 * c] = make_float4((float)t[2 * a], (float)t[2 * a + 1], (float)t[2 * b], (float)t[2 * b + 1]);
+    out[2 * c + 1] = make_float4((float)t[2 * d], (float)t[2 * d + 1], (float)t[2 * e], (float)t[2 * e + 1]);
+}
+
+// z-triplet records of the (rho, z) table for TSC (see s1r2_interp_f32).
 __global__ void k_table2_zrec(const double *__restrict__ t, int nrho, int nz, float4 *__restrict__ out)
 {
     const size_t ncell = (size_t)nrho * nz;
@@ -867,14 +884,6 @@ __global__ void __launch_bounds__(BLOCK) k_pair_t3q(MixedArgs a)
         const float4 li = __ldg(a.ilo + qi);
         const float eown = __ldg(a.ieps + qi);
         const uint32_t idown = __ldg(a.iidx + qi);
-        // this quad's softening and ids (constant over the item)
-        float E4[4];
-        uint32_t Id4[4];
-#pragma unroll
-        for (int s = 0; s < 4; s++) {
-            E4[s] = __shfl_sync(FULL, eown, qb | s);
-            Id4[s] = __shfl_sync(FULL, idown, qb | s);
-        }
         double ax = 0.0, ay = 0.0, az = 0.0;
 
         if (J0 < J1) stage_tile<BLOCK, 1>(a, J0, sp[0], se[0], sid[0], sres[0]);
@@ -910,21 +919,11 @@ __global__ void __launch_bounds__(BLOCK) k_pair_t3q(MixedArgs a)
             }
             __syncthreads();
 
-            // own i in J's frame, then the quad's four
+            // own i in J's frame
             float phx, phy, phz, plx, ply, plz;
             frame_split(pi.x, li.x, dO[0], eO[0], phx, plx);
             frame_split(pi.y, li.y, dO[1], eO[1], phy, ply);
             frame_split(pi.z, li.z, dO[2], eO[2], phz, plz);
-            float Hx[4], Hy[4], Hz[4], Lx[4], Ly[4], Lz[4];
-#pragma unroll
-            for (int s = 0; s < 4; s++) {
-                Hx[s] = __shfl_sync(FULL, phx, qb | s);
-                Hy[s] = __shfl_sync(FULL, phy, qb | s);
-                Hz[s] = __shfl_sync(FULL, phz, qb | s);
-                Lx[s] = __shfl_sync(FULL, plx, qb | s);
-                Ly[s] = __shfl_sync(FULL, ply, qb | s);
-                Lz[s] = __shfl_sync(FULL, plz, qb | s);
-            }
             float fx[4] = {0.0f, 0.0f, 0.0f, 0.0f}, fy[4] = {0.0f, 0.0f, 0.0f, 0.0f},
                   fz[4] = {0.0f, 0.0f, 0.0f, 0.0f};
             const float4 *spb = sp[buf];
@@ -932,44 +931,70 @@ __global__ void __launch_bounds__(BLOCK) k_pair_t3q(MixedArgs a)
             const uint32_t *sidb = sid[buf];
             const float4 *sresb = sres[buf];
 
-#pragma unroll 1
-            for (int jb = 0; jb < T; jb += 4) {
-                const int jj = jb + r;
-                const float4 q = spb[jj];
-                const float ej = seb[jj];
-                const uint32_t jid = sidb[jj];
-                const float4 ql = full ? sresb[jj] : make_float4(0.f, 0.f, 0.f, 0.f);
+            if (!full) {
+                // far tile pair: the quad's four i as single FP32 positions
+                float Px[4], Py[4], Pz[4];
 #pragma unroll
                 for (int s = 0; s < 4; s++) {
-                    const bool self = full && jid == Id4[s];
-                    float dx, dy, dz;
-                    if (full) {  // double-float separation
-                        dx = self ? 0.0f : (q.x - Hx[s]) + (ql.x - Lx[s]);
-                        dy = self ? 0.0f : (q.y - Hy[s]) + (ql.y - Ly[s]);
-                        dz = self ? 0.0f : (q.z - Hz[s]) + (ql.z - Lz[s]);
-                    } else {
-                        dx = q.x - (Hx[s] + Lx[s]);
-                        dy = q.y - (Hy[s] + Ly[s]);
-                        dz = q.z - (Hz[s] + Lz[s]);
+                    Px[s] = __shfl_sync(FULL, phx + plx, qb | s);
+                    Py[s] = __shfl_sync(FULL, phy + ply, qb | s);
+                    Pz[s] = __shfl_sync(FULL, phz + plz, qb | s);
+                }
+#pragma unroll 1
+                for (int jb = 0; jb < T; jb += 4) {
+                    const float4 q = spb[jb + r];
+#pragma unroll
+                    for (int s = 0; s < 4; s++) {
+                        const float dx = q.x - Px[s], dy = q.y - Py[s], dz = q.z - Pz[s];
+                        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                        const float ri = rsqrt_mufu(r2);
+                        const float w = ri * ri * ri;
+                        float Dx = 0.0f, Dy = 0.0f, Dz = 0.0f;
+                        if (ORDER != 0) t3_correction<ORDER>(a, halo, dx, dy, dz, Dx, Dy, Dz);
+                        fx[s] = fmaf(q.w, fmaf(w, dx, -Dx), fx[s]);
+                        fy[s] = fmaf(q.w, fmaf(w, dy, -Dy), fy[s]);
+                        fz[s] = fmaf(q.w, fmaf(w, dz, -Dz), fz[s]);
                     }
-                    float nx = dx, ny = dy, nz = dz;
-                    if (full && !self) {  // wrapped axes are full-path tile pairs
-                        if (wrap[0]) nx = nearest_image(dx, q.x, Hx[s], ql.x, Lx[s], L, halfL, a.halfL_lo, a.wrap_tol);
-                        if (wrap[1]) ny = nearest_image(dy, q.y, Hy[s], ql.y, Ly[s], L, halfL, a.halfL_lo, a.wrap_tol);
-                        if (wrap[2]) nz = nearest_image(dz, q.z, Hz[s], ql.z, Lz[s], L, halfL, a.halfL_lo, a.wrap_tol);
+                }
+            } else {
+                // near tile pair (rare): double-float separations, softening, the
+                // exact nearest-image decision; each i fetched from its lane per step
+#pragma unroll 1
+                for (int jb = 0; jb < T; jb += 4) {
+                    const int jj = jb + r;
+                    const float4 q = spb[jj];
+                    const float ej = seb[jj];
+                    const uint32_t jid = sidb[jj];
+                    const float4 ql = sresb[jj];
+#pragma unroll
+                    for (int s = 0; s < 4; s++) {
+                        const float hx = __shfl_sync(FULL, phx, qb | s), hy = __shfl_sync(FULL, phy, qb | s),
+                                    hz = __shfl_sync(FULL, phz, qb | s);
+                        const float lx_ = __shfl_sync(FULL, plx, qb | s), ly_ = __shfl_sync(FULL, ply, qb | s),
+                                    lz_ = __shfl_sync(FULL, plz, qb | s);
+                        const float ei = __shfl_sync(FULL, eown, qb | s);
+                        const uint32_t iid = __shfl_sync(FULL, idown, qb | s);
+                        const bool self = jid == iid;
+                        const float dx = self ? 0.0f : (q.x - hx) + (ql.x - lx_);
+                        const float dy = self ? 0.0f : (q.y - hy) + (ql.y - ly_);
+                        const float dz = self ? 0.0f : (q.z - hz) + (ql.z - lz_);
+                        float nx = dx, ny = dy, nz = dz;
+                        if (!self) {  // wrapped axes are full-path tile pairs
+                            if (wrap[0]) nx = nearest_image(dx, q.x, hx, ql.x, lx_, L, halfL, a.halfL_lo, a.wrap_tol);
+                            if (wrap[1]) ny = nearest_image(dy, q.y, hy, ql.y, ly_, L, halfL, a.halfL_lo, a.wrap_tol);
+                            if (wrap[2]) nz = nearest_image(dz, q.z, hz, ql.z, lz_, L, halfL, a.halfL_lo, a.wrap_tol);
+                        }
+                        const float r2 = fmaf(nx, nx, fmaf(ny, ny, nz * nz));
+                        const float ri = rsqrt_mufu(r2);
+                        float w = ri * ri * ri;
+                        const float bb = ei + ej;
+                        if (r2 < bb * bb) w = spline_inner_f32(r2, bb);
+                        float Dx = 0.0f, Dy = 0.0f, Dz = 0.0f;
+                        if (ORDER != 0) t3_correction<ORDER>(a, halo, dx, dy, dz, Dx, Dy, Dz);
+                        fx[s] = fmaf(q.w, fmaf(w, nx, -Dx), fx[s]);
+                        fy[s] = fmaf(q.w, fmaf(w, ny, -Dy), fy[s]);
+                        fz[s] = fmaf(q.w, fmaf(w, nz, -Dz), fz[s]);
                     }
-                    const float r2 = fmaf(nx, nx, fmaf(ny, ny, nz * nz));
-                    const float ri = rsqrt_mufu(r2);
-                    float w = ri * ri * ri;
-                    if (full) {
-                        const float b = E4[s] + ej;
-                        if (r2 < b * b) w = spline_inner_f32(r2, b);
-                    }
-                    float Dx = 0.0f, Dy = 0.0f, Dz = 0.0f;
-                    if (ORDER != 0) t3_correction<ORDER>(a, halo, dx, dy, dz, Dx, Dy, Dz);
-                    fx[s] = fmaf(q.w, fmaf(w, nx, -Dx), fx[s]);
-                    fy[s] = fmaf(q.w, fmaf(w, ny, -Dy), fy[s]);
-                    fz[s] = fmaf(q.w, fmaf(w, nz, -Dz), fz[s]);
                 }
             }
             // 4-lane transpose-reduce: lane r = 2b + c ends with the sum of
@@ -1122,11 +1147,18 @@ void s1tab_args(MixedArgs &a, const KParams &kp, const Tables &tb, cudaStream_t 
         note_launch("k_table2_f32");
         c.s1f_version = c.s1r2_version;
     }
-    if (kp.order != 0 && (c.s1rec_version != c.s1r2_version || !c.s1rec.p)) {
-        float4 *o = c.s1rec.ensure<float4>(2 * ncell);
-        k_table2_zrec<<<(unsigned)((ncell + 255) / 256), 256, 0, st>>>(tb.s1r2, tb.nrho, tb.nz, o);
-        note_launch("k_table2_zrec");
+    if (kp.order != 0 && (c.s1rec_version != c.s1r2_version || c.s1rec_order != kp.order || !c.s1rec.p)) {
+        if (kp.order == 4) {
+            float4 *o = c.s1rec.ensure<float4>(2 * ncell);
+            k_table2_zrec<<<(unsigned)((ncell + 255) / 256), 256, 0, st>>>(tb.s1r2, tb.nrho, tb.nz, o);
+            note_launch("k_table2_zrec");
+        } else {
+            float4 *o = c.s1rec.ensure<float4>(2 * ncell);
+            k_table2_cic<<<(unsigned)((ncell + 255) / 256), 256, 0, st>>>(tb.s1r2, tb.nrho, tb.nz, o);
+            note_launch("k_table2_cic");
+        }
         c.s1rec_version = c.s1r2_version;
+        c.s1rec_order = kp.order;
     }
     a.s1tab = c.s1f.as<float2>();
     a.s1rec = kp.order != 0 ? c.s1rec.as<float4>() : nullptr;

@@ -1,6 +1,9 @@
 """bench.py at N > 1 ranks: one independent realisation per rank (no
 collective on the data path), a host barrier around the timed region and the
-maximum step time over ranks. Two gloo ranks on the CPU."""
+maximum step time over ranks. Two gloo ranks on the CPU; each evaluates the
+forces of part of its own realisation with the oracle (the CPU stand-in for
+the GPU kernel), and the parent checks them against the same realisation
+built and evaluated on its own."""
 import os
 import socket
 import sys
@@ -28,9 +31,14 @@ def _rank(rank, ws, port, q):
     w, r, _ = bench.dist_env()
     dist = bench.dist_init(w)
     ps, _, _, _, _ = bench.workload(args, r)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+
+    port = pyoracle.Port(threads=1)
     bench.barrier(dist)
+    F = port.forces(port.system(0, ps.m, ps.eps, pyoracle.make_params()), ps.x, 0, 63)
     t = bench.allmax(dist, 1.0 + 2.0 * r)  # this rank's step time
-    q.put((r, w, t, ps.x[:8].copy()))
+    q.put((r, w, t, ps.x[:8].copy(), F))
     dist.destroy_process_group()
 
 
@@ -47,7 +55,21 @@ def test_two_replicas_gloo():
     for p in procs:
         p.join(timeout=60)
         assert p.exitcode == 0
-    (r0, w0, t0, x0), (r1, w1, t1, x1) = out
+    (r0, w0, t0, x0, F0), (r1, w1, t1, x1, F1) = out
     assert (r0, r1, w0, w1) == (0, 1, 2, 2)
     assert t0 == t1 == 3.0  # every rank reports the slowest rank's time
     assert not np.allclose(x0, x1)  # independent realisations (seed 1 + rank)
+    # each rank's forces are those of its own realisation, built here again
+    sys.path.insert(0, ROOT)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import bench
+    import pyoracle
+
+    sys.argv = ["bench.py", "--workload", "cfg1", "--n", "2048", "--gpus", "2"]
+    args = bench.parse()
+    port = pyoracle.Port(threads=1)
+    for r, F in ((0, F0), (1, F1)):
+        ps, _, _, _, _ = bench.workload(args, r)
+        ref = port.forces(port.system(0, ps.m, ps.eps, pyoracle.make_params()), ps.x, 0, 63)
+        np.testing.assert_array_equal(F, ref)
+    assert not np.allclose(F0, F1)
