@@ -56,6 +56,23 @@ __device__ __forceinline__ void weights(float t, float *w)
     }
 }
 
+// float4 per T^3 stencil record, one per component (48 bytes). Padding the
+// records to 64 bytes, so that two of the three float4 come in one 256-bit
+// load, was 13 % (trilinear) and 17 % (tricubic) slower: the larger table
+// loses L1 hits.
+constexpr int T3R = 3;
+
+// Two float4 of a 32-byte aligned record in one 256-bit load (sm_100+):
+// the L1 data path, which bounds the table kernels, sees one request per
+// record instead of two. The S1xR2 CIC and TSC records are 32 bytes: CIC
+// 2.71e11 -> 3.53e11 and TSC 1.06e11 -> 1.31e11 pairs/s at N = 2^20.
+__device__ __forceinline__ void ldg_v8(const float4 *p, float4 &a, float4 &b)
+{
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(p));
+}
+
 // w . v for the 4 z taps of a z-row record.
 __device__ __forceinline__ float dot4(const float *w, float4 v)
 {
@@ -323,13 +340,13 @@ __global__ void __launch_bounds__(BLOCK) k_pair_t3(MixedArgs a)
                             if (ORDER == 4) {
                                 // z-row records: the 4 z taps of one (x, y) row, per
                                 // component, in 3 float4 (48 B), 16 rows per pair
-                                const float4 *rbase = a.t3r + 3 * ((bx * E + by) * E + bz);
+                                const float4 *rbase = a.t3r + T3R * ((bx * E + by) * E + bz);
 #pragma unroll
                                 for (int aa = 0; aa < 4; aa++) {
                                     float rx = 0.0f, ry = 0.0f, rz = 0.0f;
 #pragma unroll
                                     for (int bb = 0; bb < 4; bb++) {
-                                        const float4 *r = rbase + 3 * (aa * E + bb) * E;
+                                        const float4 *r = rbase + T3R * (aa * E + bb) * E;
                                         const float4 vx = __ldg(r), vy = __ldg(r + 1), vz = __ldg(r + 2);
                                         rx = fmaf(wy[bb], dot4(wz, vx), rx);
                                         ry = fmaf(wy[bb], dot4(wz, vy), ry);
@@ -344,10 +361,10 @@ __global__ void __launch_bounds__(BLOCK) k_pair_t3(MixedArgs a)
                                 // component, in 3 float4 (48 B), 2 records per pair
                                 const float q00 = wy[0] * wz[0], q01 = wy[0] * wz[1], q10 = wy[1] * wz[0],
                                             q11 = wy[1] * wz[1];
-                                const float4 *rbase = a.t3r + 3 * ((bx * E + by) * E + bz);
+                                const float4 *rbase = a.t3r + T3R * ((bx * E + by) * E + bz);
 #pragma unroll
                                 for (int aa = 0; aa < 2; aa++) {
-                                    const float4 *r = rbase + 3 * aa * E * E;
+                                    const float4 *r = rbase + T3R * aa * E * E;
                                     const float4 vx = __ldg(r), vy = __ldg(r + 1), vz = __ldg(r + 2);
                                     Dx = fmaf(wx[aa], fmaf(q11, vx.w, fmaf(q10, vx.z, fmaf(q01, vx.y, q00 * vx.x))), Dx);
                                     Dy = fmaf(wx[aa], fmaf(q11, vy.w, fmaf(q10, vy.z, fmaf(q01, vy.y, q00 * vy.x))), Dy);
@@ -459,8 +476,8 @@ __device__ __forceinline__ void s1r2_interp_f32(const float2 *__restrict__ T, co
         STEPS_CHECK_IDX(ra, nrho - 1, CK_S1_CELL);
         STEPS_CHECK_IDX(iz0, nz, CK_S1_CELL);
         // record (ir0, iz0): rows ir0, ir0 + 1 x cells iz0, iz0 + 1 (periodic)
-        const float4 *rec = R + 2 * ((size_t)ra * nz + iz0);
-        const float4 r0 = __ldg(rec), r1 = __ldg(rec + 1);
+        float4 r0, r1;
+        ldg_v8(R + 2 * ((size_t)ra * nz + iz0), r0, r1);  // 32-byte records, 256-byte aligned base
         const float w00 = (1.0f - fr) * (1.0f - fz), w10 = fr * (1.0f - fz), w01 = (1.0f - fr) * fz, w11 = fr * fz;
         Dr = w00 * r0.x + w10 * r1.x + w01 * r0.z + w11 * r1.z;
         Dz = w00 * r0.y + w10 * r1.y + w01 * r0.w + w11 * r1.w;
@@ -480,8 +497,8 @@ __device__ __forceinline__ void s1r2_interp_f32(const float2 *__restrict__ T, co
         for (int r = 0; r < 3; r++) STEPS_CHECK_IDX(ir[r], nrho, CK_S1_CELL);
 #pragma unroll
         for (int r = 0; r < 3; r++) {  // record (ir, iz1): cells iz1 - 1, iz1, iz1 + 1
-            const float4 *rec = R + 2 * ((size_t)ir[r] * nz + iz1);
-            const float4 v01 = __ldg(rec), v2 = __ldg(rec + 1);
+            float4 v01, v2;
+            ldg_v8(R + 2 * ((size_t)ir[r] * nz + iz1), v01, v2);  // 32-byte records
             const float sr_ = fmaf(wz[2], v2.x, fmaf(wz[1], v01.z, wz[0] * v01.x));
             const float sz_ = fmaf(wz[2], v2.y, fmaf(wz[1], v01.w, wz[0] * v01.y));
             Dr = fmaf(wr[r], sr_, Dr);
@@ -790,14 +807,14 @@ __device__ __forceinline__ void t3_correction(const MixedArgs &a, bool halo, flo
                         CK_T3_CELL))
             bx = by = bz = 0;
 #endif
-        const float4 *rbase = a.t3r + 3 * ((bx * E + by) * E + bz);
+        const float4 *rbase = a.t3r + T3R * ((bx * E + by) * E + bz);
         if (ORDER == 4) {  // z-row records
 #pragma unroll
             for (int aa = 0; aa < 4; aa++) {
                 float rx = 0.0f, ry = 0.0f, rz = 0.0f;
 #pragma unroll
                 for (int bb = 0; bb < 4; bb++) {
-                    const float4 *r = rbase + 3 * (aa * E + bb) * E;
+                    const float4 *r = rbase + T3R * (aa * E + bb) * E;
                     const float4 vx = __ldg(r), vy = __ldg(r + 1), vz = __ldg(r + 2);
                     rx = fmaf(wy[bb], dot4(wz, vx), rx);
                     ry = fmaf(wy[bb], dot4(wz, vy), ry);
@@ -811,7 +828,7 @@ __device__ __forceinline__ void t3_correction(const MixedArgs &a, bool halo, flo
             const float q00 = wy[0] * wz[0], q01 = wy[0] * wz[1], q10 = wy[1] * wz[0], q11 = wy[1] * wz[1];
 #pragma unroll
             for (int aa = 0; aa < 2; aa++) {
-                const float4 *r = rbase + 3 * aa * E * E;
+                const float4 *r = rbase + T3R * aa * E * E;
                 const float4 vx = __ldg(r), vy = __ldg(r + 1), vz = __ldg(r + 2);
                 Dx = fmaf(wx[aa], fmaf(q11, vx.w, fmaf(q10, vx.z, fmaf(q01, vx.y, q00 * vx.x))), Dx);
                 Dy = fmaf(wx[aa], fmaf(q11, vy.w, fmaf(q10, vy.z, fmaf(q01, vy.y, q00 * vy.x))), Dy);
@@ -1054,7 +1071,7 @@ KernelFn t3_kernel(const KParams &kp, int threads, int ipt, size_t *dyn_smem, in
     return kp.order == 4 ? pick_t3<4>(threads, ipt) : pick_t3<2>(threads, ipt);
 }
 
-// Stencil records of the haloed table, 3 float4 per record (one per
+// Stencil records of the haloed table, T3R = 3 float4 per record (one per
 // component), record (i, j, k) of the ext^3 grid:
 //   tricubic: z row  -- cells (i, j, k..k+3)
 //   trilinear: (y, z) quad -- cells (i, j, k), (i, j, k+1), (i, j+1, k), (i, j+1, k+1)
@@ -1071,7 +1088,8 @@ __global__ void k_table_records(const double *__restrict__ t, int ng, int halo, 
         const size_t s = ((size_t)pmod(i - halo, ng) * ng + pmod(j + dj - halo, ng)) * ng + pmod(k + dk - halo, ng);
         for (int comp = 0; comp < 3; comp++) v[comp][q] = (float)t[3 * s + comp];
     }
-    for (int comp = 0; comp < 3; comp++) out[3 * c + comp] = make_float4(v[comp][0], v[comp][1], v[comp][2], v[comp][3]);
+    for (int comp = 0; comp < T3R; comp++)
+        out[T3R * c + comp] = make_float4(v[comp][0], v[comp][1], v[comp][2], v[comp][3]);
 }
 
 // Halo of the FP32 table copies: tile pairs whose stencils stay within it
@@ -1102,7 +1120,7 @@ const float4 *t3_table_records(const Tables &tb, int order, cudaStream_t st)
     const size_t ext = (size_t)tb.t3_ng + 2 * t3_halo(tb.t3_ng);
     const size_t ncell = ext * ext * ext;
     if (c.t3r_version != c.t3_version || c.t3r_order != order || !c.t3r.p) {
-        float4 *o = c.t3r.ensure<float4>(3 * ncell);
+        float4 *o = c.t3r.ensure<float4>(T3R * ncell);
         k_table_records<<<(unsigned)((ncell + 255) / 256), 256, 0, st>>>(tb.t3, tb.t3_ng, t3_halo(tb.t3_ng), order,
                                                                           o);
         note_launch("k_table_records");
