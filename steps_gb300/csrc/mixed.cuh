@@ -47,7 +47,8 @@ struct MixedArgs {
     float ih, u0;       // continuous cell index u(d) = d * ih + u0, ih = ng / L, u0 = ng/2 - 1/2
     int wcap;           // cells of the shared-memory table window
     int halo, ext;      // the FP32 copy is haloed: ext^3 cells, ext = ng + 2 halo
-    const float4 *t3r;  // stencil records of the haloed copy (3 float4 per cell)
+    const float4 *t3r;  // stencil records of the haloed copy: x, y components (2 float4 per cell)
+    const float4 *t3rz; // ... and the z component (1 float4 per cell)
     // S1xR2 (rho, z) correction table (FP32 float2 copy) and its geometry
     const float2 *s1tab;
     const float4 *s1rec;  // records of s1tab: whole CIC stencils (32 bytes), TSC z triplets

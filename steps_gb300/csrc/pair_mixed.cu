@@ -559,6 +559,7 @@ void forces_mixed(const KParams &kp, const Tables &tb, const double *x, const do
     a.wcap = 0;
     a.halo = a.ext = 0;
     a.t3r = nullptr;
+    a.t3rz = nullptr;
     a.s1tab = nullptr;
     a.s1rec = nullptr;
     a.nrho = a.nz = 0;

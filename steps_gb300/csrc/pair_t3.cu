@@ -56,11 +56,12 @@ __device__ __forceinline__ void weights(float t, float *w)
     }
 }
 
-// float4 per T^3 stencil record, one per component (48 bytes). Padding the
-// records to 64 bytes, so that two of the three float4 come in one 256-bit
-// load, was 13 % (trilinear) and 17 % (tricubic) slower: the larger table
-// loses L1 hits.
-constexpr int T3R = 3;
+// T^3 stencil records, one float4 per component, in two arrays of the same
+// cell index: the x and y components as one 32-byte record (a.t3r, read with
+// one 256-bit load) and the z component as one 16-byte record (a.t3rz): two
+// L1 requests per record instead of three, in the same 48 bytes per cell.
+// (Records padded to 64 bytes for the same purpose were 13-17 % slower: the
+// larger table loses L1 hits.)
 
 // Two float4 of a 32-byte aligned record in one 256-bit load (sm_100+):
 // the L1 data path, which bounds the table kernels, sees one request per
@@ -340,14 +341,16 @@ __global__ void __launch_bounds__(BLOCK) k_pair_t3(MixedArgs a)
                             if (ORDER == 4) {
                                 // z-row records: the 4 z taps of one (x, y) row, per
                                 // component, in 3 float4 (48 B), 16 rows per pair
-                                const float4 *rbase = a.t3r + T3R * ((bx * E + by) * E + bz);
+                                const int cb = (bx * E + by) * E + bz;
 #pragma unroll
                                 for (int aa = 0; aa < 4; aa++) {
                                     float rx = 0.0f, ry = 0.0f, rz = 0.0f;
 #pragma unroll
                                     for (int bb = 0; bb < 4; bb++) {
-                                        const float4 *r = rbase + T3R * (aa * E + bb) * E;
-                                        const float4 vx = __ldg(r), vy = __ldg(r + 1), vz = __ldg(r + 2);
+                                        const int cr = cb + (aa * E + bb) * E;
+                                        float4 vx, vy;
+                                        ldg_v8(a.t3r + 2 * (size_t)cr, vx, vy);
+                                        const float4 vz = __ldg(a.t3rz + cr);
                                         rx = fmaf(wy[bb], dot4(wz, vx), rx);
                                         ry = fmaf(wy[bb], dot4(wz, vy), ry);
                                         rz = fmaf(wy[bb], dot4(wz, vz), rz);
@@ -361,11 +364,13 @@ __global__ void __launch_bounds__(BLOCK) k_pair_t3(MixedArgs a)
                                 // component, in 3 float4 (48 B), 2 records per pair
                                 const float q00 = wy[0] * wz[0], q01 = wy[0] * wz[1], q10 = wy[1] * wz[0],
                                             q11 = wy[1] * wz[1];
-                                const float4 *rbase = a.t3r + T3R * ((bx * E + by) * E + bz);
+                                const int cb = (bx * E + by) * E + bz;
 #pragma unroll
                                 for (int aa = 0; aa < 2; aa++) {
-                                    const float4 *r = rbase + T3R * aa * E * E;
-                                    const float4 vx = __ldg(r), vy = __ldg(r + 1), vz = __ldg(r + 2);
+                                    const int cr = cb + aa * E * E;
+                                    float4 vx, vy;
+                                    ldg_v8(a.t3r + 2 * (size_t)cr, vx, vy);
+                                    const float4 vz = __ldg(a.t3rz + cr);
                                     Dx = fmaf(wx[aa], fmaf(q11, vx.w, fmaf(q10, vx.z, fmaf(q01, vx.y, q00 * vx.x))), Dx);
                                     Dy = fmaf(wx[aa], fmaf(q11, vy.w, fmaf(q10, vy.z, fmaf(q01, vy.y, q00 * vy.x))), Dy);
                                     Dz = fmaf(wx[aa], fmaf(q11, vz.w, fmaf(q10, vz.z, fmaf(q01, vz.y, q00 * vz.x))), Dz);
@@ -807,15 +812,17 @@ __device__ __forceinline__ void t3_correction(const MixedArgs &a, bool halo, flo
                         CK_T3_CELL))
             bx = by = bz = 0;
 #endif
-        const float4 *rbase = a.t3r + T3R * ((bx * E + by) * E + bz);
+        const int cb = (bx * E + by) * E + bz;
         if (ORDER == 4) {  // z-row records
 #pragma unroll
             for (int aa = 0; aa < 4; aa++) {
                 float rx = 0.0f, ry = 0.0f, rz = 0.0f;
 #pragma unroll
                 for (int bb = 0; bb < 4; bb++) {
-                    const float4 *r = rbase + T3R * (aa * E + bb) * E;
-                    const float4 vx = __ldg(r), vy = __ldg(r + 1), vz = __ldg(r + 2);
+                    const int cr = cb + (aa * E + bb) * E;
+                    float4 vx, vy;
+                    ldg_v8(a.t3r + 2 * (size_t)cr, vx, vy);
+                    const float4 vz = __ldg(a.t3rz + cr);
                     rx = fmaf(wy[bb], dot4(wz, vx), rx);
                     ry = fmaf(wy[bb], dot4(wz, vy), ry);
                     rz = fmaf(wy[bb], dot4(wz, vz), rz);
@@ -828,8 +835,10 @@ __device__ __forceinline__ void t3_correction(const MixedArgs &a, bool halo, flo
             const float q00 = wy[0] * wz[0], q01 = wy[0] * wz[1], q10 = wy[1] * wz[0], q11 = wy[1] * wz[1];
 #pragma unroll
             for (int aa = 0; aa < 2; aa++) {
-                const float4 *r = rbase + T3R * aa * E * E;
-                const float4 vx = __ldg(r), vy = __ldg(r + 1), vz = __ldg(r + 2);
+                const int cr = cb + aa * E * E;
+                float4 vx, vy;
+                ldg_v8(a.t3r + 2 * (size_t)cr, vx, vy);
+                const float4 vz = __ldg(a.t3rz + cr);
                 Dx = fmaf(wx[aa], fmaf(q11, vx.w, fmaf(q10, vx.z, fmaf(q01, vx.y, q00 * vx.x))), Dx);
                 Dy = fmaf(wx[aa], fmaf(q11, vy.w, fmaf(q10, vy.z, fmaf(q01, vy.y, q00 * vy.x))), Dy);
                 Dz = fmaf(wx[aa], fmaf(q11, vz.w, fmaf(q10, vz.z, fmaf(q01, vz.y, q00 * vz.x))), Dz);
@@ -1071,11 +1080,12 @@ KernelFn t3_kernel(const KParams &kp, int threads, int ipt, size_t *dyn_smem, in
     return kp.order == 4 ? pick_t3<4>(threads, ipt) : pick_t3<2>(threads, ipt);
 }
 
-// Stencil records of the haloed table, T3R = 3 float4 per record (one per
-// component), record (i, j, k) of the ext^3 grid:
+// Stencil records of the haloed table, one float4 per component, record
+// (i, j, k) of the ext^3 grid (x and y in out[2c], out[2c + 1], z in outz[c]):
 //   tricubic: z row  -- cells (i, j, k..k+3)
 //   trilinear: (y, z) quad -- cells (i, j, k), (i, j, k+1), (i, j+1, k), (i, j+1, k+1)
-__global__ void k_table_records(const double *__restrict__ t, int ng, int halo, int order, float4 *__restrict__ out)
+__global__ void k_table_records(const double *__restrict__ t, int ng, int halo, int order, float4 *__restrict__ out,
+                                float4 *__restrict__ outz)
 {
     const int ext = ng + 2 * halo;
     const size_t ncell = (size_t)ext * ext * ext;
@@ -1088,8 +1098,9 @@ __global__ void k_table_records(const double *__restrict__ t, int ng, int halo, 
         const size_t s = ((size_t)pmod(i - halo, ng) * ng + pmod(j + dj - halo, ng)) * ng + pmod(k + dk - halo, ng);
         for (int comp = 0; comp < 3; comp++) v[comp][q] = (float)t[3 * s + comp];
     }
-    for (int comp = 0; comp < T3R; comp++)
-        out[T3R * c + comp] = make_float4(v[comp][0], v[comp][1], v[comp][2], v[comp][3]);
+    out[2 * c] = make_float4(v[0][0], v[0][1], v[0][2], v[0][3]);
+    out[2 * c + 1] = make_float4(v[1][0], v[1][1], v[1][2], v[1][3]);
+    outz[c] = make_float4(v[2][0], v[2][1], v[2][2], v[2][3]);
 }
 
 // Halo of the FP32 table copies: tile pairs whose stencils stay within it
@@ -1120,9 +1131,9 @@ const float4 *t3_table_records(const Tables &tb, int order, cudaStream_t st)
     const size_t ext = (size_t)tb.t3_ng + 2 * t3_halo(tb.t3_ng);
     const size_t ncell = ext * ext * ext;
     if (c.t3r_version != c.t3_version || c.t3r_order != order || !c.t3r.p) {
-        float4 *o = c.t3r.ensure<float4>(T3R * ncell);
+        float4 *o = c.t3r.ensure<float4>(3 * ncell);  // 2 ncell xy records, then ncell z records
         k_table_records<<<(unsigned)((ncell + 255) / 256), 256, 0, st>>>(tb.t3, tb.t3_ng, t3_halo(tb.t3_ng), order,
-                                                                          o);
+                                                                          o, o + 2 * ncell);
         note_launch("k_table_records");
         c.t3r_version = c.t3_version;
         c.t3r_order = order;
@@ -1140,9 +1151,12 @@ void t3_args(MixedArgs &a, const KParams &kp, const Tables &tb, cudaStream_t st)
     a.halo = t3_halo(tb.t3_ng);
     a.ext = tb.t3_ng + 2 * a.halo;
     a.t3r = nullptr;
+    a.t3rz = nullptr;
     if (kp.is_periodic >= 2) {
         a.t3f = t3_table_f32(tb, st);
         a.t3r = t3_table_records(tb, kp.order == 4 ? 4 : 2, st);
+        const size_t ext = (size_t)tb.t3_ng + 2 * t3_halo(tb.t3_ng);
+        a.t3rz = a.t3r + 2 * ext * ext * ext;
         a.ih = (float)((double)tb.t3_ng / kp.L);
         a.u0 = (float)((double)tb.t3_ng * 0.5 - 0.5);
     }
