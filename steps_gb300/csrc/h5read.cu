@@ -29,13 +29,17 @@ struct H5File {
     int so = 8, sl = 8;  // sizes of offsets and lengths
     uint64_t base = 0;   // base address
 
+    // [at, at + n) lies in the file (no wrap-around for corrupt addresses)
+    bool has(uint64_t at, uint64_t n) const { return at <= b.size() && n <= b.size() - at; }
     uint64_t u(uint64_t at, int n) const
     {
-        if (at + (uint64_t)n > b.size()) fail(STEPS_E_ARG, "hdf5: truncated file");
+        if (!has(at, (uint64_t)n)) fail(STEPS_E_ARG, "hdf5: truncated file");
         uint64_t v = 0;
         for (int k = n - 1; k >= 0; k--) v = (v << 8) | b[at + k];
         return v;
     }
+    // the 4-byte signature at `at` (bounds-checked)
+    bool magic(uint64_t at, const char *sig) const { return has(at, 4) && memcmp(&b[at], sig, 4) == 0; }
     uint64_t off(uint64_t at) const { return u(at, so); }
     uint64_t len(uint64_t at) const { return u(at, sl); }
     uint64_t addr(uint64_t a) const { return a + base; }
@@ -75,7 +79,7 @@ std::vector<Message> object_messages(const H5File &f, uint64_t oh)
 std::string heap_name(const H5File &f, uint64_t heap, uint64_t offset)
 {
     const uint64_t h = f.addr(heap);
-    if (memcmp(&f.b[h], "HEAP", 4) != 0) fail(STEPS_E_ARG, "hdf5: bad local heap");
+    if (!f.magic(h, "HEAP")) fail(STEPS_E_ARG, "hdf5: bad local heap");
     const uint64_t data = f.addr(f.off(h + 8 + 2 * f.sl));
     std::string s;
     for (uint64_t p = data + offset; p < f.b.size() && f.b[p]; p++) s.push_back((char)f.b[p]);
@@ -89,7 +93,7 @@ bool group_lookup(const H5File &f, uint64_t btree, uint64_t heap, const std::str
 {
     if (depth > 64) fail(STEPS_E_ARG, "hdf5: group B-tree too deep");
     const uint64_t t = f.addr(btree);
-    if (memcmp(&f.b[t], "TREE", 4) != 0 || f.u(t + 4, 1) != 0) fail(STEPS_E_ARG, "hdf5: bad group B-tree node");
+    if (!f.magic(t, "TREE") || f.u(t + 4, 1) != 0) fail(STEPS_E_ARG, "hdf5: bad group B-tree node");
     const int level = (int)f.u(t + 5, 1);
     const int used = (int)f.u(t + 6, 2);
     uint64_t p = t + 8 + 2 * f.so;  // key 0, child 0, key 1, child 1, ..., key `used`
@@ -101,7 +105,7 @@ bool group_lookup(const H5File &f, uint64_t btree, uint64_t heap, const std::str
             continue;
         }
         const uint64_t s = f.addr(child);
-        if (memcmp(&f.b[s], "SNOD", 4) != 0) fail(STEPS_E_ARG, "hdf5: bad symbol table node");
+        if (!f.magic(s, "SNOD")) fail(STEPS_E_ARG, "hdf5: bad symbol table node");
         const int nsym = (int)f.u(s + 6, 2);
         const uint64_t entry = 2 * (uint64_t)f.so + 24;  // name offset, header address, cache type + pad, scratch
         for (int e = 0; e < nsym; e++) {
@@ -196,9 +200,12 @@ Dataset read_dataset_header(const H5File &f, uint64_t oh)
     if (d.cls == 0 && d.size != 1 && d.size != 2 && d.size != 4 && d.size != 8)
         fail(STEPS_E_ARG, "hdf5: unsupported integer size");
     uint64_t count = 1;
-    for (uint64_t v : d.dims) count *= v;
+    for (uint64_t v : d.dims) {
+        if (v != 0 && count > f.b.size() / v) fail(STEPS_E_ARG, "hdf5: dataspace larger than the file");
+        count *= v;
+    }
     if (count * (uint64_t)d.size != d.bytes) fail(STEPS_E_ARG, "hdf5: storage size does not match the dataspace");
-    if (d.data + d.bytes > f.b.size()) fail(STEPS_E_ARG, "hdf5: truncated dataset");
+    if (!f.has(d.data, d.bytes)) fail(STEPS_E_ARG, "hdf5: truncated dataset");
     return d;
 }
 

@@ -67,3 +67,52 @@ def test_errors(tmp_path):
     assert "not an HDF5 file" in str(e.value)
     with pytest.raises(S.StepsError):
         S.h5_read(str(tmp_path / "missing.h5"), "/a")
+
+
+_FUZZ = r"""
+import os, sys
+import numpy as np
+sys.path.insert(0, {root!r})
+import steps_gb300 as S
+
+src = open({path!r}, "rb").read()
+tmp = {tmp!r}
+rng = np.random.default_rng(7)
+cases = [src[:n] for n in range(0, len(src), max(1, len(src) // 97))]
+# the structures: the superblock and first group at the start, the dataset's
+# object header and the other groups after the raw data at the end
+spans = [(0, min(len(src), 1024)), (max(0, len(src) - 3072), len(src))]
+for _ in range(400):  # random bytes of the structures overwritten
+    b = bytearray(src)
+    for _ in range(int(rng.integers(1, 6))):
+        lo, hi = spans[int(rng.integers(0, 2))]
+        b[int(rng.integers(lo, hi))] = int(rng.integers(0, 256))
+    cases.append(bytes(b))
+ok = err = 0
+for k, c in enumerate(cases):
+    with open(tmp, "wb") as f:
+        f.write(c)
+    try:
+        S.h5_read(tmp, {dataset!r})
+        ok += 1
+    except S.StepsError:
+        err += 1
+print("done", ok, err)
+"""
+
+
+@pytest.mark.parametrize("name,dataset", [("t3_table_ng17.h5", "/t3_ewald/T3_EWALD_FORCE_TABLE"),
+                                          ("s1r2_table.h5", "/s1r2_ewald/S1R2_EWALD_FORCE_TABLE")])
+def test_truncated_and_corrupt_files_fail_cleanly(tmp_path, name, dataset):
+    """Truncated files and files with random bytes of their structures
+    overwritten either read or return STEPS_E_ARG: the reader never reads
+    outside the file (run in a child process, so a crash would show)."""
+    import subprocess
+    import sys
+
+    code = _FUZZ.format(root=ROOT, path=os.path.join(GOLDEN, name), tmp=str(tmp_path / "f.h5"), dataset=dataset)
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert r.stdout.strip().startswith("done"), r.stdout[-2000:]
+    ok, err = (int(v) for v in r.stdout.split()[1:3])
+    assert err > 150  # the truncations and most corruptions
